@@ -1,0 +1,160 @@
+/*
+ * nsgb.h -- C ABI of the GB300 (sm_103a) single-device Chorin-projection solver.
+ *
+ * Each entry point replaces one operation of the reference JAX solver
+ * (helmhlotz/ns_solver_jax_differential_distributed, file NS_solver.py); the
+ * comment above it names the reference symbol and lines it stands in for.
+ *
+ * Conventions
+ *  - Fields are float32, C-contiguous, caller-owned DEVICE pointers.  A vector
+ *    field is (2, N, N): component 0 = u_x, 1 = u_y; axis 1 = x (rows, index i),
+ *    axis 2 = y (contiguous, index j) -- the reference's layout
+ *    (NS_solver.py:116, 676-679).
+ *  - N is a power of two, 16 <= N <= 4096.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  All calls are
+ *    asynchronous with respect to the host unless stated otherwise.
+ *  - Every call returns an int status (NSGB_OK = 0); on failure the
+ *    thread-local nsgb_last_error() string says why.  No C++ exception crosses
+ *    this boundary.
+ *  - `theta` is a device pointer to theta_len float32 values: [A, B] (the
+ *    reference's forcing parameters, NS_solver.py:623) or [A, B, nu], in which
+ *    case theta[2] replaces the viscosity.
+ *  - Workspace buffers are caller-owned device memory of at least the size
+ *    the matching *_workspace_bytes() query returns.  A plan owns only its
+ *    constant tables (twiddles, squared wavenumbers).
+ */
+#ifndef NSGB_H
+#define NSGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSGB_OK 0
+#define NSGB_ERR_INVALID_ARG 1
+#define NSGB_ERR_UNSUPPORTED_N 2
+#define NSGB_ERR_CUDA 3
+#define NSGB_ERR_OOM 4
+#define NSGB_ERR_WORKSPACE 5
+#define NSGB_ERR_NONFINITE 6
+
+#define NSGB_SCHEME_CENTRAL 0 /* CentralAdvection, NS_solver.py:468-477 */
+#define NSGB_SCHEME_UPWIND 1  /* UpwindAdvection,  NS_solver.py:480-488 */
+
+typedef struct nsgb_plan nsgb_plan;
+
+/* Physical and time parameters of one solve: the reference's Phys (nu, mu0,
+ * sigma0, C; NS_solver.py:99-101), Time.dt (NS_solver.py:108-110), the grid
+ * length L (NS_solver.py:112-117) and the advection scheme name. */
+typedef struct nsgb_phys {
+  double L;
+  double nu;
+  double dt;
+  double mu0;
+  double sigma0;
+  double C;
+  int scheme; /* NSGB_SCHEME_* */
+} nsgb_phys;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int nsgb_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* nsgb_last_error(void);
+
+/* Create the constant tables of one grid size on the current device: the
+ * FFT twiddles and the squared wavenumbers k = 2*pi*fftfreq(N, dx) of
+ * SpectralPoissonSolver.__init__ (NS_solver.py:517-521).  A plan is immutable
+ * after set-up and may be shared by streams. */
+int nsgb_plan_create(int N, double L, nsgb_plan** plan);
+int nsgb_plan_destroy(nsgb_plan* plan);
+
+/* Launch shapes used by the plan's kernels: stencil tile (tw x th cells),
+ * rows per CTA of the row FFTs, k-rows per CTA of the column FFT.  All
+ * powers of two; 0 keeps the current value.  Chosen by the autotuner. */
+int nsgb_plan_set_tiles(nsgb_plan* plan, int tw, int th, int rows_per_cta, int cols_per_cta);
+int nsgb_plan_get_tiles(const nsgb_plan* plan, int out[4]);
+
+/* Bytes of workspace for nsgb_poisson / nsgb_projector_step / nsgb_step. */
+size_t nsgb_poisson_workspace_bytes(const nsgb_plan* plan);
+size_t nsgb_step_workspace_bytes(const nsgb_plan* plan);
+/* Bytes of workspace for nsgb_rollout over `steps` steps. */
+size_t nsgb_rollout_workspace_bytes(const nsgb_plan* plan, int steps);
+/* Bytes of workspace for nsgb_rollout_grad with checkpoints every `every` steps. */
+size_t nsgb_rollout_grad_workspace_bytes(const nsgb_plan* plan, int steps, int every);
+
+/* PeriodicDifferentialOps.grad (NS_solver.py:243-247): central gradient.
+ * f: (N,N); gx, gy: (N,N). */
+int nsgb_grad(const nsgb_plan* plan, const float* f, float* gx, float* gy, void* stream);
+
+/* PeriodicDifferentialOps.laplacian (NS_solver.py:249-255): 5-point Laplacian. */
+int nsgb_laplacian(const nsgb_plan* plan, const float* f, float* out, void* stream);
+
+/* DifferentialOps.divergence / divergence_vec (NS_solver.py:206-218):
+ * u: (2,N,N) -> out: (N,N). */
+int nsgb_divergence(const nsgb_plan* plan, const float* u, float* out, void* stream);
+
+/* AdvectionScheme.advect (NS_solver.py:453-488): -(u.grad) field with the
+ * central gradient (CentralAdvection, :474-477) or first-order upwind
+ * differences (PeriodicDifferentialOps.upwind_advect, :257-265). */
+int nsgb_advect(const nsgb_plan* plan, int scheme, const float* field, const float* ux,
+                const float* uy, float* out, void* stream);
+
+/* SpectralPoissonSolver.__call__ (NS_solver.py:523-527): p = Re ifft2(
+ * -fft2(rhs) * inv_k2) with p_hat[0,0] = 0, i.e. lap(p) = rhs.  Hand-written
+ * R2C / C2R FFTs; `workspace` holds the half spectrum. */
+int nsgb_poisson(const nsgb_plan* plan, const float* rhs, float* p, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
+/* GaussianForcingField.__call__ (NS_solver.py:637-640): writes the (2,N,N)
+ * force field at time t (fy = 0). */
+int nsgb_forcing(const nsgb_plan* plan, const nsgb_phys* phys, const float* theta, int theta_len,
+                 float t, float* f_out, void* stream);
+
+/* ChorinProjector.step (NS_solver.py:671-697) with an explicit force field
+ * f (2,N,N): u* = u + dt(nu lap u + adv(u) + f); p = poisson(div(u*)/dt);
+ * u_out = u* - dt grad p.  nu, dt, scheme are taken from `phys`. */
+int nsgb_projector_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u,
+                        const float* f, float* u_out, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+/* SingleCoreNSSolver.step (NS_solver.py:727-730): one step with the Gaussian
+ * forcing at time t. */
+int nsgb_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, const float* theta,
+              int theta_len, float t, float* u_out, void* workspace, size_t workspace_bytes,
+              void* stream);
+
+/* SingleCoreNSSolver.rollout (NS_solver.py:732-750): `steps` steps from u0 with
+ * t = i*dt, accumulating J += dt * sum(u*f) * dx^2 on the state before each
+ * step.  Writes u_final (2,N,N) and *J (one float, device).  The projection of
+ * each step is fused into the next step's stencil; steps are replayed as
+ * CUDA-graph chunks when use_graph != 0. */
+int nsgb_rollout(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta,
+                 int theta_len, int steps, float* u_final, float* J, void* workspace,
+                 size_t workspace_bytes, int use_graph, void* stream);
+
+/* Phases of nsgb_rollout_grad. */
+#define NSGB_GRAD_FORWARD 1  /* rollout with checkpoints, J, u_final */
+#define NSGB_GRAD_BACKWARD 2 /* adjoint sweep: dJ/dtheta (and dJ/du0) */
+
+/* jax.grad of the rollout objective (SingleCoreNSSolver.jit_gradient,
+ * NS_solver.py:725, generalised to a given u0): hand-written discrete adjoint
+ * of the whole step with checkpoints of the state every `every` steps and
+ * recomputation of each segment during the backward sweep.
+ * `phases` selects NSGB_GRAD_FORWARD and/or NSGB_GRAD_BACKWARD; a backward
+ * call must follow a forward call with the same arguments and workspace
+ * (the checkpoints live in the workspace).  The forward phase writes *J and,
+ * if non-NULL, u_final; the backward phase writes dJdtheta[theta_len] and, if
+ * non-NULL, dJdu0 (2,N,N). */
+int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
+                      const float* theta, int theta_len, int steps, int every, int phases,
+                      float* J, float* u_final, float* dJdtheta, float* dJdu0, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NSGB_H */

@@ -1,0 +1,282 @@
+// Discrete adjoint of one Chorin step (the reverse-mode derivative that
+// jax.grad takes of SingleCoreNSSolver.objective, NS_solver.py:725, 742-756).
+//
+// Forward step s (exact arithmetic):  v = u + dt (nu L u + A(u) + f_s),
+// u_{s+1} = Pr v with Pr = I - G P^-1 D, and J += jscale <u_x, f_x>,
+// jscale = dt dx^2.  With periodic central differences G^T = -D and the
+// spectral inverse Laplacian symmetric, so Pr^T = Pr and the adjoint recursion
+// (lambda_S = 0) is
+//   mu_s      = Pr lambda_{s+1}
+//   lambda_s  = mu_s + dt (nu L mu_s + A'(u_s)^T mu_s) + jscale (f_x, 0)
+//   dJ/dA,B  += sum_cells (jscale u_x + dt mu_x) dfx/dA,B
+//   dJ/dnu   += dt <mu_s, L u_s>
+// A'(u)^T for central advection A_c = -(u_x Gx u_c + u_y Gy u_c):
+//   (A'^T mu)_x = -(mu_x Gx u_x + mu_y Gx u_y) + Gx(mu_x u_x) + Gy(mu_x u_y)
+//   (A'^T mu)_y = -(mu_x Gy u_x + mu_y Gy u_y) + Gx(mu_y u_x) + Gy(mu_y u_y)
+// and for upwind differences (masks m = [u >= 0] held fixed, as the
+// derivative of jnp.where is taken):
+//   (A'^T mu)_c = -(mu_x DX u_c... ) terms as below, with the transposed
+//   one-sided operator (DX^m)^T w (i) = [(2m_i - 1) w_i - m_{i+1} w_{i+1}
+//   + (1 - m_{i-1}) w_{i-1}] / dx.
+// The projection Pr lambda_{s+1} reuses the forward machinery: the previous
+// adjoint kernel wrote rhs = div(lambda_{s+1}) / dt, the FFT kernels solved for
+// p, and this kernel applies mu = lambda - dt grad p on its tile.
+#include "nsgb_internal.h"
+
+namespace nsgb {
+
+template <int SCHEME>
+__global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
+  extern __shared__ float sm[];
+  const StepConsts& c = a.c;
+  const int N = c.N, M = N - 1;
+  const size_t NN = (size_t)N * N;
+  const int TW = a.tw, TH = a.th;
+  const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
+  const int tx = threadIdx.x, ty = threadIdx.y, nty = blockDim.y;
+  const int PW = TW + 6, PH = TH + 6;
+  const int UW = TW + 4, UH = TH + 4;
+  const int SW = TW + 2, SH = TH + 2;
+  float* sP = sm;
+  float* sMx = sP + PH * PW;
+  float* sMy = sMx + UH * UW;
+  float* sUx = sMy + UH * UW;
+  float* sUy = sUx + UH * UW;
+  float* sLx = sUy + UH * UW;
+  float* sLy = sLx + SH * SW;
+  float* sF = sLy + SH * SW;   // fx for the SH rows of the lambda tile
+  float* sDA = sF + SH;        // dfx/dA for the TH interior rows
+  float* sDB = sDA + TH;       // dfx/dB
+  float* sRed = sDB + TH;      // 3 x 8
+
+  const float dt = c.dt;
+  const float jscale = c.jscale;  // float32(dt * dx^2) = dJ/du_x / f_x
+  const float nu = (a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float t = fmul((float)a.step, dt);
+  const float A = __ldg(a.theta), B = __ldg(a.theta + 1);
+
+  {
+    const int tid = ty * 32 + tx;
+    const ForcingRow fr = forcing_time(A, B, t, c);
+    if (tid < SH) {
+      sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
+    } else if (tid >= 64 && tid < 64 + TH) {
+      const int r = tid - 64;
+      float fx, dmu, dsig;
+      forcing_fx_grad((i0 + r) & M, fr, c, fx, dmu, dsig);
+      const float twopi = 6.28318548202514648f;
+      const float argA = fmul(fmul(twopi, A), t);
+      const float argB = fmul(fmul(twopi, B), t);
+      const float cb = cosf(argB);
+      // d mu/dA = cos(2 pi A t) 2 pi t ;  d sig/dB = -2 cos sin (2 pi B t) 2 pi t
+      sDA[r] = dmu * (cosf(argA) * twopi * t);
+      sDB[r] = dsig * (-2.0f * cb * sinf(argB) * twopi * t);
+    }
+  }
+
+  const bool has_lam = a.lam != nullptr;
+  const bool has_p = a.p != nullptr;
+  if (has_p) {
+    for (int r = ty; r < PH; r += nty) {
+      const float* row = a.p + (size_t)((i0 - 3 + r) & M) * N;
+      for (int cc = tx; cc < PW; cc += 32) sP[r * PW + cc] = __ldg(row + ((j0 - 3 + cc) & M));
+    }
+  }
+  for (int r = ty; r < UH; r += nty) {
+    const size_t rowoff = (size_t)((i0 - 2 + r) & M) * N;
+    for (int cc = tx; cc < UW; cc += 32) {
+      const size_t g = rowoff + ((j0 - 2 + cc) & M);
+      const int o = r * UW + cc;
+      sUx[o] = __ldg(a.u + g);
+      sUy[o] = __ldg(a.u + NN + g);
+      sMx[o] = has_lam ? __ldg(a.lam + g) : 0.0f;
+      sMy[o] = has_lam ? __ldg(a.lam + NN + g) : 0.0f;
+    }
+  }
+  __syncthreads();
+
+  if (has_p) {  // mu = lambda - dt grad p
+    for (int r = ty; r < UH; r += nty) {
+      for (int cc = tx; cc < UW; cc += 32) {
+        const int op = (r + 1) * PW + (cc + 1);
+        const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
+        const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
+        const int o = r * UW + cc;
+        sMx[o] = fsub(sMx[o], fmul(dt, px));
+        sMy[o] = fsub(sMy[o], fmul(dt, py));
+      }
+    }
+    __syncthreads();
+  }
+
+  // theta sensitivities on the interior cells
+  float gA = 0.f, gB = 0.f, gN = 0.f;
+  for (int r = ty; r < TH; r += nty) {
+    for (int cc = tx; cc < TW; cc += 32) {
+      const int o = (r + 2) * UW + (cc + 2);
+      const float w = jscale * sUx[o] + dt * sMx[o];
+      gA += w * sDA[r];
+      gB += w * sDB[r];
+      const float lux = (sUx[o - UW] + sUx[o + UW] + sUx[o + 1] + sUx[o - 1] - 4.0f * sUx[o]) / c.dx2;
+      const float luy = (sUy[o - UW] + sUy[o + UW] + sUy[o + 1] + sUy[o - 1] - 4.0f * sUy[o]) / c.dx2;
+      gN += dt * (sMx[o] * lux + sMy[o] * luy);
+    }
+  }
+
+  // lambda_s on the tile + 1 halo
+  const float inv_h2 = 1.0f / c.h2;
+  const float inv_h1 = 1.0f / c.h1;
+  for (int r = ty; r < SH; r += nty) {
+    for (int cc = tx; cc < SW; cc += 32) {
+      const int o = (r + 1) * UW + (cc + 1);
+      const int n = o + UW, s = o - UW, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
+      const float mx = sMx[o], my = sMy[o];
+      const float lmx = (sMx[s] + sMx[n] + sMx[e] + sMx[w] - 4.0f * mx) / c.dx2;
+      const float lmy = (sMy[s] + sMy[n] + sMy[e] + sMy[w] - 4.0f * my) / c.dx2;
+      float atx, aty;
+      if (SCHEME == NSGB_SCHEME_CENTRAL) {
+        const float gxux = (sUx[n] - sUx[s]) * inv_h2, gxuy = (sUy[n] - sUy[s]) * inv_h2;
+        const float gyux = (sUx[e] - sUx[w]) * inv_h2, gyuy = (sUy[e] - sUy[w]) * inv_h2;
+        atx = -(mx * gxux + my * gxuy) + (sMx[n] * sUx[n] - sMx[s] * sUx[s]) * inv_h2 +
+              (sMx[e] * sUy[e] - sMx[w] * sUy[w]) * inv_h2;
+        aty = -(mx * gyux + my * gyuy) + (sMy[n] * sUx[n] - sMy[s] * sUx[s]) * inv_h2 +
+              (sMy[e] * sUy[e] - sMy[w] * sUy[w]) * inv_h2;
+      } else {
+        const float uxo = sUx[o], uyo = sUy[o];
+        const bool mxo = uxo >= 0.f, myo = uyo >= 0.f;
+        // one-sided differences of u at o (the forward's dfx, dfy)
+        const float dxux = (mxo ? uxo - sUx[s] : sUx[n] - uxo) * inv_h1;
+        const float dxuy = (mxo ? uyo - sUy[s] : sUy[n] - uyo) * inv_h1;
+        const float dyux = (myo ? uxo - sUx[w] : sUx[e] - uxo) * inv_h1;
+        const float dyuy = (myo ? uyo - sUy[w] : sUy[e] - uyo) * inv_h1;
+        atx = -(mx * dxux + my * dxuy);
+        aty = -(mx * dyux + my * dyuy);
+        // transposed one-sided operators applied to w = mu_c u_x (x) and mu_c u_y (y)
+        const bool mxn = sUx[n] >= 0.f, mxs = sUx[s] >= 0.f;
+        const bool mye = sUy[e] >= 0.f, myw = sUy[w] >= 0.f;
+#define NSGB_DXT(MU)                                                                    \
+  (((mxo ? MU[o] * uxo : -MU[o] * uxo) - (mxn ? MU[n] * sUx[n] : 0.f) +                \
+    (mxs ? 0.f : MU[s] * sUx[s])) * inv_h1)
+#define NSGB_DYT(MU)                                                                    \
+  (((myo ? MU[o] * uyo : -MU[o] * uyo) - (mye ? MU[e] * sUy[e] : 0.f) +                \
+    (myw ? 0.f : MU[w] * sUy[w])) * inv_h1)
+        atx -= NSGB_DXT(sMx) + NSGB_DYT(sMx);
+        aty -= NSGB_DXT(sMy) + NSGB_DYT(sMy);
+#undef NSGB_DXT
+#undef NSGB_DYT
+      }
+      sLx[r * SW + cc] = mx + dt * (nu * lmx + atx) + jscale * sF[r];
+      sLy[r * SW + cc] = my + dt * (nu * lmy + aty);
+    }
+  }
+  __syncthreads();
+
+  for (int r = ty; r < TH; r += nty) {
+    for (int cc = tx; cc < TW; cc += 32) {
+      const int o = (r + 1) * SW + (cc + 1);
+      const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
+      a.lam_out[g] = sLx[o];
+      a.lam_out[NN + g] = sLy[o];
+      const float gx = fdiv(fsub(sLx[o + SW], sLx[o - SW]), c.h2);
+      const float gy = fdiv(fsub(sLy[o + 1], sLy[o - 1]), c.h2);
+      a.rhs[g] = fdiv(fadd(gx, gy), dt);
+    }
+  }
+
+  gA = warp_sum(gA);
+  gB = warp_sum(gB);
+  gN = warp_sum(gN);
+  if (tx == 0) {
+    sRed[ty] = gA;
+    sRed[8 + ty] = gB;
+    sRed[16 + ty] = gN;
+  }
+  __syncthreads();
+  if (ty == 0) {
+    float v0 = (tx < nty) ? sRed[tx] : 0.f;
+    float v1 = (tx < nty) ? sRed[8 + tx] : 0.f;
+    float v2 = (tx < nty) ? sRed[16 + tx] : 0.f;
+    v0 = warp_sum(v0);
+    v1 = warp_sum(v1);
+    v2 = warp_sum(v2);
+    if (tx == 0) {
+      const int nblk = gridDim.x * gridDim.y;
+      float* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
+      gp[0] = v0;
+      gp[1] = v1;
+      gp[2] = v2;
+    }
+  }
+}
+
+static size_t adjoint_smem(int tw, int th) {
+  const size_t f = (size_t)(th + 6) * (tw + 6) + 4 * (size_t)(th + 4) * (tw + 4) +
+                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 2 * th + 24;
+  return f * sizeof(float);
+}
+
+template <int SCHEME>
+static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_adjoint<SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    configured = true;
+  }
+  const dim3 grid(a.c.N / a.tw, a.c.N / a.th);
+  k_adjoint<SCHEME><<<grid, dim3(32, 8), adjoint_smem(a.tw, a.th), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
+  return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_t<NSGB_SCHEME_CENTRAL>(a, st)
+                                         : launch_adjoint_t<NSGB_SCHEME_UPWIND>(a, st);
+}
+
+// Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double).
+__global__ void k_greduce(const float* __restrict__ gpart, int nblk, int nrows,
+                          double* __restrict__ gacc) {
+  __shared__ double red[3][256];
+  for (int row = 0; row < nrows; ++row) {
+    const float* base = gpart + (size_t)row * nblk * 3;
+    double v0 = 0, v1 = 0, v2 = 0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+      v0 += base[3 * b];
+      v1 += base[3 * b + 1];
+      v2 += base[3 * b + 2];
+    }
+    red[0][threadIdx.x] = v0;
+    red[1][threadIdx.x] = v1;
+    red[2][threadIdx.x] = v2;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        red[0][threadIdx.x] += red[0][threadIdx.x + s];
+        red[1][threadIdx.x] += red[1][threadIdx.x + s];
+        red[2][threadIdx.x] += red[2][threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      gacc[0] += red[0][0];
+      gacc[1] += red[1][0];
+      gacc[2] += red[2][0];
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_greduce(const float* gpart, int nblk, int nrows, double* gacc, cudaStream_t st) {
+  if (nrows > 0) k_greduce<<<1, 256, 0, st>>>(gpart, nblk, nrows, gacc);
+  return cudaGetLastError();
+}
+
+__global__ void k_gfinal(const double* __restrict__ gacc, int theta_len, float* __restrict__ dJ) {
+  for (int k = 0; k < theta_len; ++k) dJ[k] = (float)gacc[k];
+}
+
+cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st) {
+  k_gfinal<<<1, 1, 0, st>>>(gacc, theta_len, dJ);
+  return cudaGetLastError();
+}
+
+}  // namespace nsgb

@@ -1,0 +1,160 @@
+// Block-level FFT building blocks for power-of-two lengths 16..4096.
+//
+// A transform of length N is carried by T = N/E threads, each holding E =
+// min(16, N) complex values in registers.  Thread j holds elements j + s*T
+// (s = 0..E-1) on entry and X[j + s*T] on exit, so the first pass reads and
+// the last pass writes "natural" strided positions; rows stored contiguously
+// in global memory are therefore loaded and stored fully coalesced.
+//
+// The transform is the radix-16 Stockham autosort algorithm (a final pass of
+// radix 2/4/8 when log2(N) is not a multiple of 4).  Between passes the values
+// are exchanged through shared memory, split into real and imaginary planes
+// and padded by one word every 16 (index i -> i + i/16), which makes the pass
+// writes bank-conflict free.  Twiddles come from a table W_N[m] =
+// exp(-2 pi i m / N) computed on the host in double precision.
+#pragma once
+
+#include "nsgb_common.cuh"
+
+namespace nsgb {
+namespace fft {
+
+__host__ __device__ constexpr int ept(int N) { return N < 16 ? N : 16; }
+__host__ __device__ constexpr int padlen(int N) { return N + N / 16 + 4; }
+__device__ __forceinline__ int pad(int i) { return i + (i >> 4); }
+
+template <int R>
+__device__ __forceinline__ constexpr int bitrev(int k) {
+  int r = 0;
+  for (int b = 1; b < R; b <<= 1) {
+    r = (r << 1) | (k & 1);
+    k >>= 1;
+  }
+  return r;
+}
+
+// cos / sin of 2*pi*m/16 for m = 0..7
+__device__ __forceinline__ float c16(int m) {
+  switch (m) {
+    case 0: return 1.0f;
+    case 1: return 0.923879532511286756f;
+    case 2: return 0.707106781186547524f;
+    case 3: return 0.382683432365089772f;
+    case 4: return 0.0f;
+    case 5: return -0.382683432365089772f;
+    case 6: return -0.707106781186547524f;
+    default: return -0.923879532511286756f;
+  }
+}
+__device__ __forceinline__ float s16(int m) {
+  switch (m) {
+    case 0: return 0.0f;
+    case 1: return 0.382683432365089772f;
+    case 2: return 0.707106781186547524f;
+    case 3: return 0.923879532511286756f;
+    case 4: return 1.0f;
+    case 5: return 0.923879532511286756f;
+    case 6: return 0.707106781186547524f;
+    default: return 0.382683432365089772f;
+  }
+}
+
+// d * exp(-+ 2 pi i m / 16): forward uses the minus sign.
+template <bool INV>
+__device__ __forceinline__ float2 rot16(float2 d, int m) {
+  if (m == 0) return d;
+  if (m == 4) return INV ? make_float2(-d.y, d.x) : make_float2(d.y, -d.x);
+  const float c = c16(m);
+  const float s = INV ? s16(m) : -s16(m);
+  return make_float2(d.x * c - d.y * s, d.x * s + d.y * c);
+}
+
+// In-register DFT of size R (2, 4, 8 or 16): natural order in and out.
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 (&a)[R]) {
+#pragma unroll
+  for (int len = R; len >= 2; len >>= 1) {
+    const int half = len >> 1;
+#pragma unroll
+    for (int s = 0; s < R; s += len) {
+#pragma unroll
+      for (int t = 0; t < half; ++t) {
+        const float2 u = a[s + t];
+        const float2 v = a[s + t + half];
+        a[s + t] = cadd(u, v);
+        a[s + t + half] = rot16<INV>(csub(u, v), t * (16 / len));
+      }
+    }
+  }
+  float2 b[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) b[k] = a[bitrev<R>(k)];
+#pragma unroll
+  for (int k = 0; k < R; ++k) a[k] = b[k];
+}
+
+// One Stockham pass (stride NS) and, recursively, the remaining passes.
+template <int N, int NS, bool INV>
+__device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sre,
+                                     float* __restrict__ sim, int j,
+                                     const float2* __restrict__ tw) {
+  constexpr int E = ept(N);
+  constexpr int T = N / E;
+  constexpr int REM = N / NS;
+  constexpr int RP = REM >= 16 ? 16 : REM;
+  constexpr int Q = E / RP;
+  constexpr bool LAST = (NS * RP == N);
+  constexpr int TWS = N / (NS * RP);
+#pragma unroll
+  for (int q = 0; q < Q; ++q) {
+    const int b = j + q * T;
+    float2 x[RP];
+#pragma unroll
+    for (int r = 0; r < RP; ++r) x[r] = a[q + r * Q];
+    if constexpr (NS > 1) {
+      const int bm = b & (NS - 1);
+#pragma unroll
+      for (int r = 1; r < RP; ++r) {
+        float2 w = __ldg(&tw[bm * r * TWS]);
+        if (INV) w.y = -w.y;
+        x[r] = cmul(x[r], w);
+      }
+    }
+    dft<RP, INV>(x);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int r = 0; r < RP; ++r) a[q + r * Q] = x[r];
+    } else {
+      const int base = (b / NS) * (NS * RP) + (b & (NS - 1));
+#pragma unroll
+      for (int r = 0; r < RP; ++r) {
+        const int idx = pad(base + r * NS);
+        sre[idx] = x[r].x;
+        sim[idx] = x[r].y;
+      }
+    }
+  }
+  if constexpr (!LAST) {
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+      const int idx = pad(j + s * T);
+      a[s] = make_float2(sre[idx], sim[idx]);
+    }
+    __syncthreads();
+    pass<N, NS * RP, INV>(a, sre, sim, j, tw);
+  }
+}
+
+// Full FFT of length N (unnormalised; INV uses exp(+2 pi i ...)).  Every
+// thread of the CTA must call it: it synchronises the block between passes.
+// On return the exchange buffer is free for reuse without a further barrier
+// only after the caller's next __syncthreads.
+template <int N, bool INV>
+__device__ __forceinline__ void block_fft(float2 (&a)[ept(N)], float* sre, float* sim, int j,
+                                          const float2* __restrict__ tw) {
+  pass<N, 1, INV>(a, sre, sim, j, tw);
+}
+
+}  // namespace fft
+}  // namespace nsgb

@@ -1,0 +1,276 @@
+// FFT-Poisson kernels: the hand-written replacement of SpectralPoissonSolver
+// (NS_solver.py:507-527).
+//
+// The real N x N right-hand side is transformed in two passes:
+//   rows (along y, contiguous): two real rows a, b are packed as a + i b, one
+//     complex length-N FFT gives both half spectra X_a[k], X_b[k], k=0..N/2.
+//     The half spectrum is stored transposed, spec[k][i] (k = 0..N/2-1,
+//     i contiguous), with the real DC and Nyquist values of row i packed as
+//     spec[0][i] = (X_i[0], X_i[N/2]).  spec holds N*N/2 complex = N*N floats,
+//     the size of the real field.
+//   columns (along x): each spec[k] row is transformed, multiplied by
+//     -1/|k|^2 (0 at k = 0; NS_solver.py:521, 525-526), transformed back and
+//     written in place.  The packed row k = 0 carries two real-valued columns,
+//     which are separated with Hermitian symmetry, scaled by their own
+//     multipliers and recombined.
+//   rows again: the inverse two-for-one C2R transform writes p.
+// All scale factors (the 1/2 of the two-for-one split and the 1/N^2 of ifft2)
+// are powers of two folded into the spectral multiplier, so they round
+// exactly.
+#include "nsgb_fft.cuh"
+#include "nsgb_internal.h"
+
+namespace nsgb {
+
+using fft::ept;
+using fft::pad;
+using fft::padlen;
+
+// Per-pair exchange buffer stride in floats (re plane + im plane + a small
+// skew so the buffers of different pairs start in different banks).
+template <int N>
+__host__ __device__ constexpr int pair_stride() {
+  return 2 * padlen(N) + 4;
+}
+
+// ---------------------------------------------------------------- rows fwd --
+// blockDim = (T, P): P row pairs per CTA, rows [blockIdx.x * 2P, +2P).
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_fwd(const float* __restrict__ rhs,
+                                                   float2* __restrict__ spec,
+                                                   const float2* __restrict__ tw) {
+  constexpr int E = ept(N);
+  constexpr int T = N / E;
+  constexpr int H = N / 2;
+  constexpr int PL = padlen(N);
+  extern __shared__ float smem[];
+  const int j = threadIdx.x, pp = threadIdx.y, P = blockDim.y;
+  float* sre = smem + pp * pair_stride<N>();
+  float* sim = sre + PL;
+  const int RB = 2 * P;
+  const int i0 = blockIdx.x * RB;
+  const float* ra = rhs + (size_t)(i0 + 2 * pp) * N;
+  const float* rb = ra + N;
+
+  float2 a[E];
+#pragma unroll
+  for (int s = 0; s < E; ++s) a[s] = make_float2(__ldg(ra + j + s * T), __ldg(rb + j + s * T));
+  fft::block_fft<N, false>(a, sre, sim, j, tw);
+  __syncthreads();
+#pragma unroll
+  for (int s = 0; s < E; ++s) {
+    const int idx = pad(j + s * T);
+    sre[idx] = a[s].x;
+    sim[idx] = a[s].y;
+  }
+  __syncthreads();
+
+  const int tid = threadIdx.y * T + threadIdx.x;
+  const int nth = T * P;
+  for (int e = tid; e < RB * H; e += nth) {
+    const int r = e & (RB - 1);
+    const int k = e / RB;
+    const float* pre = smem + (r >> 1) * pair_stride<N>();
+    const float* pim = pre + PL;
+    float2 out;
+    if (k == 0) {
+      out = (r & 1) ? make_float2(2.0f * pim[pad(0)], 2.0f * pim[pad(H)])
+                    : make_float2(2.0f * pre[pad(0)], 2.0f * pre[pad(H)]);
+    } else {
+      const float zr = pre[pad(k)], zi = pim[pad(k)];
+      const float wr = pre[pad(N - k)], wi = pim[pad(N - k)];
+      out = (r & 1) ? make_float2(zi + wi, wr - zr)   // 2 X_b[k]
+                    : make_float2(zr + wr, zi - wi);  // 2 X_a[k]
+    }
+    spec[(size_t)k * N + i0 + r] = out;
+  }
+}
+
+// ----------------------------------------------------------------- columns --
+// Spectral multiplier  -1/(kx^2 + ky^2) * scale, 0 where the sum is 0.
+__device__ __forceinline__ float poisson_mult(float k2x, float k2y, float scale) {
+  const float den = k2x + k2y;
+  const float inv = (den == 0.0f) ? 0.0f : __fdiv_rn(1.0f, den);
+  return -inv * scale;
+}
+
+// blockDim = (T, KB): KB spectrum rows per CTA, rows [blockIdx.x * KB, +KB).
+template <int N>
+__global__ void __launch_bounds__(512) k_cols(float2* __restrict__ spec,
+                                               const float2* __restrict__ tw,
+                                               const float* __restrict__ k2,
+                                               float scale) {
+  constexpr int E = ept(N);
+  constexpr int T = N / E;
+  constexpr int H = N / 2;
+  constexpr int PL = padlen(N);
+  extern __shared__ float smem[];
+  const int j = threadIdx.x, y = threadIdx.y;
+  float* sre = smem + y * pair_stride<N>();
+  float* sim = sre + PL;
+  const int ky = blockIdx.x * blockDim.y + y;
+  float2* row = spec + (size_t)ky * N;
+
+  float2 a[E];
+#pragma unroll
+  for (int s = 0; s < E; ++s) a[s] = row[j + s * T];
+  fft::block_fft<N, false>(a, sre, sim, j, tw);
+
+  const float k2y = __ldg(k2 + ky);
+  if (blockIdx.x == 0) {
+    // The CTA holding ky = 0: its packed row needs C[-m] from other threads.
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+      const int idx = pad(j + s * T);
+      sre[idx] = a[s].x;
+      sim[idx] = a[s].y;
+    }
+    __syncthreads();
+    if (ky == 0) {
+      const float k2n = __ldg(k2 + H);
+#pragma unroll
+      for (int s = 0; s < E; ++s) {
+        const int m = j + s * T;
+        const int mm = pad((N - m) & (N - 1));
+        const float2 cm = make_float2(sre[mm], -sim[mm]);  // conj(C[-m])
+        const float k2x = __ldg(k2 + m);
+        const float g0 = poisson_mult(k2x, 0.0f, scale);
+        const float gn = poisson_mult(k2x, k2n, scale);
+        // C' = ((C + conj(C[-m])) g0 + (C - conj(C[-m])) gn) / 2
+        const float2 sp = cadd(a[s], cm), sm = csub(a[s], cm);
+        a[s] = make_float2(0.5f * (sp.x * g0 + sm.x * gn), 0.5f * (sp.y * g0 + sm.y * gn));
+      }
+    } else {
+#pragma unroll
+      for (int s = 0; s < E; ++s) {
+        const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
+        a[s] = make_float2(a[s].x * g, a[s].y * g);
+      }
+    }
+    __syncthreads();
+  } else {
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+      const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
+      a[s] = make_float2(a[s].x * g, a[s].y * g);
+    }
+  }
+
+  fft::block_fft<N, true>(a, sre, sim, j, tw);
+#pragma unroll
+  for (int s = 0; s < E; ++s) row[j + s * T] = a[s];
+}
+
+// ---------------------------------------------------------------- rows inv --
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_inv(const float2* __restrict__ spec,
+                                                   float* __restrict__ p,
+                                                   const float2* __restrict__ tw) {
+  constexpr int E = ept(N);
+  constexpr int T = N / E;
+  constexpr int H = N / 2;
+  constexpr int PL = padlen(N);
+  extern __shared__ float smem[];
+  const int j = threadIdx.x, pp = threadIdx.y, P = blockDim.y;
+  const int RB = 2 * P;
+  const int i0 = blockIdx.x * RB;
+  const int tid = threadIdx.y * T + threadIdx.x;
+  const int nth = T * P;
+
+  // Stage the RB half-spectrum rows: pair buffer (r>>1) holds X_a at [0,H)
+  // and X_b at [H, N).
+  for (int e = tid; e < RB * H; e += nth) {
+    const int r = e & (RB - 1);
+    const int k = e / RB;
+    const float2 v = __ldg(spec + (size_t)k * N + i0 + r);
+    float* pre = smem + (r >> 1) * pair_stride<N>();
+    const int idx = pad((r & 1) * H + k);
+    pre[idx] = v.x;
+    pre[PL + idx] = v.y;
+  }
+  __syncthreads();
+
+  float* sre = smem + pp * pair_stride<N>();
+  float* sim = sre + PL;
+  float2 a[E];
+#pragma unroll
+  for (int s = 0; s < E; ++s) {
+    const int m = j + s * T;
+    float2 z;
+    if (m == 0) {
+      z = make_float2(sre[pad(0)], sre[pad(H)]);
+    } else if (m == H) {
+      z = make_float2(sim[pad(0)], sim[pad(H)]);
+    } else if (m < H) {
+      const float2 xa = make_float2(sre[pad(m)], sim[pad(m)]);
+      const float2 xb = make_float2(sre[pad(H + m)], sim[pad(H + m)]);
+      z = make_float2(xa.x - xb.y, xa.y + xb.x);  // X_a + i X_b
+    } else {
+      const float2 xa = make_float2(sre[pad(N - m)], sim[pad(N - m)]);
+      const float2 xb = make_float2(sre[pad(H + N - m)], sim[pad(H + N - m)]);
+      z = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj(X_a) + i conj(X_b)
+    }
+    a[s] = z;
+  }
+  __syncthreads();
+  fft::block_fft<N, true>(a, sre, sim, j, tw);
+  float* ra = p + (size_t)(i0 + 2 * pp) * N;
+  float* rb = ra + N;
+#pragma unroll
+  for (int s = 0; s < E; ++s) {
+    ra[j + s * T] = a[s].x;
+    rb[j + s * T] = a[s].y;
+  }
+}
+
+// ------------------------------------------------------------- launchers --
+template <int N>
+static cudaError_t launch_poisson_fft(const FftLaunch& L, cudaStream_t st) {
+  constexpr int T = N / ept(N);
+  const int P = L.rows_per_cta / 2;
+  const int KB = L.cols_per_cta;
+  const size_t smem_rows = (size_t)P * pair_stride<N>() * sizeof(float);
+  const size_t smem_cols = (size_t)KB * pair_stride<N>() * sizeof(float);
+  static bool configured = false;  // per-process attribute set-up (idempotent)
+  if (!configured) {
+    cudaFuncSetAttribute(k_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    configured = true;
+  }
+  if (L.rhs) {
+    k_rows_fwd<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.rhs, L.spec, L.tw);
+  }
+  if (L.do_cols) {
+    k_cols<N><<<(N / 2) / KB, dim3(T, KB), smem_cols, st>>>(L.spec, L.tw, L.k2, L.scale);
+  }
+  if (L.p) {
+    k_rows_inv<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.spec, L.p, L.tw);
+  }
+  return cudaGetLastError();
+}
+
+size_t fft_rows_smem_bytes(int N, int rows_per_cta) {
+  return (size_t)(rows_per_cta / 2) * (2 * padlen(N) + 4) * sizeof(float);
+}
+size_t fft_cols_smem_bytes(int N, int cols_per_cta) {
+  return (size_t)cols_per_cta * (2 * padlen(N) + 4) * sizeof(float);
+}
+
+cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st) {
+  switch (N) {
+    case 16: return launch_poisson_fft<16>(L, st);
+    case 32: return launch_poisson_fft<32>(L, st);
+    case 64: return launch_poisson_fft<64>(L, st);
+    case 128: return launch_poisson_fft<128>(L, st);
+    case 256: return launch_poisson_fft<256>(L, st);
+    case 512: return launch_poisson_fft<512>(L, st);
+    case 1024: return launch_poisson_fft<1024>(L, st);
+    case 2048: return launch_poisson_fft<2048>(L, st);
+    case 4096: return launch_poisson_fft<4096>(L, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+}  // namespace nsgb

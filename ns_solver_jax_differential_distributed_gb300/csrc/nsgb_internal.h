@@ -1,0 +1,92 @@
+// Internal interfaces between the kernel translation units and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "nsgb_common.cuh"
+
+namespace nsgb {
+
+// ------------------------------------------------------------------ FFT --
+struct FftLaunch {
+  const float* rhs = nullptr;  // rows forward input (nullptr: skip the pass)
+  float2* spec = nullptr;      // transposed half spectrum, (N/2) x N complex
+  bool do_cols = true;         // column transform + Poisson multiplier
+  float* p = nullptr;          // rows inverse output (nullptr: skip the pass)
+  const float2* tw = nullptr;  // twiddles W_N[m], m = 0..N-1
+  const float* k2 = nullptr;   // squared wavenumbers, N entries
+  float scale = 0.f;           // 1 / (2 N^2)
+  int rows_per_cta = 8;        // even, power of two
+  int cols_per_cta = 2;        // power of two
+};
+cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st);
+size_t fft_rows_smem_bytes(int N, int rows_per_cta);
+size_t fft_cols_smem_bytes(int N, int cols_per_cta);
+
+// --------------------------------------------------------------- stencil --
+enum StencilMode : int {
+  MODE_ROLLOUT = 0,  // Gaussian forcing computed per row, J partial per block
+  MODE_FIELD = 1,    // explicit (2,N,N) force field, no J
+};
+
+struct StencilArgs {
+  const float* us = nullptr;     // (2,N,N) u* of the pending projection (or u if p == nullptr)
+  const float* p = nullptr;      // (N,N) pressure of the pending projection, or nullptr
+  const float* f = nullptr;      // (2,N,N) force field (MODE_FIELD)
+  float* us_out = nullptr;       // (2,N,N) next u*
+  float* rhs = nullptr;          // (N,N) div(u*)/dt
+  float* u_out = nullptr;        // optional (2,N,N): the projected state u^n
+  float* jpart = nullptr;        // per-block partial sums of u_x * f_x, [step][nblk]
+  const float* theta = nullptr;  // device theta
+  int theta_len = 2;
+  const int* step_ctr = nullptr;  // device step base (nullptr: 0); step = base + step_fixed
+  int step_fixed = 0;
+  int t_from_step = 1;  // t = float(step) * dt (rollout) or t_fixed (single step)
+  float t_fixed = 0.f;
+  int scheme = 0;
+  int tw = 64, th = 16;  // tile shape (powers of two, <= N)
+  StepConsts c;
+};
+cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st);
+int stencil_nblocks(int N, int tw, int th);
+
+// u_out = us - dt * grad(p)  (NS_solver.py:696-697)
+cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
+                           cudaStream_t st);
+// Sum the per-block partials of each step in a fixed order and accumulate J.
+cudaError_t launch_jreduce(const float* jpart, int nblk, int steps, double* jsteps, float* J,
+                           double jscale, cudaStream_t st);
+// *step_ctr = value (add = false) or *step_ctr += value (add = true)
+cudaError_t launch_step_counter(int* step_ctr, int value, bool add, cudaStream_t st);
+
+// Single operators of PeriodicDifferentialOps / AdvectionScheme.
+cudaError_t launch_grad(const float* f, float* gx, float* gy, const StepConsts& c, cudaStream_t st);
+cudaError_t launch_laplacian(const float* f, float* out, const StepConsts& c, cudaStream_t st);
+cudaError_t launch_divergence(const float* u, float* out, const StepConsts& c, cudaStream_t st);
+cudaError_t launch_advect(int scheme, const float* fld, const float* ux, const float* uy, float* out,
+                          const StepConsts& c, cudaStream_t st);
+cudaError_t launch_forcing_field(const float* theta, int theta_len, float t, float* f,
+                                 const StepConsts& c, cudaStream_t st);
+
+// ---------------------------------------------------------------- adjoint --
+struct AdjointArgs {
+  const float* lam = nullptr;    // (2,N,N) lambda_{s+1} (before projection), or nullptr (zero)
+  const float* p = nullptr;      // (N,N) pressure of the pending adjoint projection, or nullptr
+  const float* u = nullptr;      // (2,N,N) forward state u_s
+  float* lam_out = nullptr;      // (2,N,N) lambda_s
+  float* rhs = nullptr;          // (N,N) div(lambda_s)/dt
+  float* gpart = nullptr;        // per-block partial theta sensitivities, [step][nblk][3]
+  const float* theta = nullptr;
+  int theta_len = 2;
+  int step = 0;                  // forward step index s (forcing time t = s*dt)
+  int gslot = 0;                 // row of gpart to write
+  int scheme = 0;
+  int tw = 64, th = 16;
+  StepConsts c;
+};
+cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
+cudaError_t launch_greduce(const float* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
+cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st);
+
+}  // namespace nsgb

@@ -1,0 +1,374 @@
+// Fused stencil kernel of the Chorin step and the single operators of
+// PeriodicDifferentialOps / AdvectionScheme.
+//
+// k_stencil processes one TH x TW tile of the grid per CTA (blockDim 32 x 8).
+// It stages the pending pressure p with a 3-cell halo and the pending u* with
+// a 2-cell halo in shared memory (periodic wrap by index masking), then
+//   1. finishes the previous step's projection  u^n = u* - dt grad p
+//      (NS_solver.py:696-697) on the tile + 2-cell halo,
+//   2. accumulates the objective partial  sum u^n_x f_x  (NS_solver.py:746),
+//   3. forms u*^{n+1} = u^n + dt (nu lap u^n + adv(u^n) + f)  on the tile +
+//      1-cell halo (NS_solver.py:685-689, 249-265, 474-477),
+//   4. writes u*^{n+1} and rhs = div(u*^{n+1}) / dt for the tile
+//      (NS_solver.py:692-693, 206-210).
+// The elementwise arithmetic keeps the reference's operation order with
+// explicitly rounded intrinsics (no FMA contraction), so it rounds exactly
+// like the reference's float32 array expressions.
+#include "nsgb_internal.h"
+
+namespace nsgb {
+
+// 5-point Laplacian at centre o of a tile with row pitch W (NS_solver.py:249-255).
+__device__ __forceinline__ float lap5(const float* s, int o, int W, const StepConsts& c) {
+  const float f = s[o];
+  const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
+  return fdiv(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f)), c.dx2);
+}
+
+// -(u . grad) field at centre o (NS_solver.py:474-477 central, :257-265 upwind).
+template <int SCHEME>
+__device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, float uy,
+                                      const StepConsts& c) {
+  const float f = s[o];
+  const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
+  if (SCHEME == NSGB_SCHEME_CENTRAL) {
+    const float gx = fdiv(fsub(right, left), c.h2);
+    const float gy = fdiv(fsub(up, down), c.h2);
+    return -fadd(fmul(ux, gx), fmul(uy, gy));
+  } else {
+    const float dfx = fdiv(ux >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1);
+    const float dfy = fdiv(uy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1);
+    return -fadd(fmul(ux, dfx), fmul(uy, dfy));
+  }
+}
+
+template <int SCHEME, int MODE>
+__global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
+  extern __shared__ float sm[];
+  const StepConsts& c = a.c;
+  const int N = c.N, M = N - 1;
+  const size_t NN = (size_t)N * N;
+  const int TW = a.tw, TH = a.th;
+  const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
+  const int tx = threadIdx.x, ty = threadIdx.y, nty = blockDim.y;
+  const int PW = TW + 6, PH = TH + 6;
+  const int UW = TW + 4, UH = TH + 4;
+  const int SW = TW + 2, SH = TH + 2;
+  float* sP = sm;
+  float* sUx = sP + PH * PW;
+  float* sUy = sUx + UH * UW;
+  float* sSx = sUy + UH * UW;
+  float* sSy = sSx + SH * SW;
+  float* sF = sSy + SH * SW;
+  float* sRed = sF + SH;
+
+  int step = 0;
+  float t = a.t_fixed;
+  if (MODE == MODE_ROLLOUT) {
+    step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed;
+    if (a.t_from_step) t = fmul((float)step, c.dt);
+  }
+  const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+
+  if (MODE == MODE_ROLLOUT) {
+    const int tid = ty * 32 + tx;
+    if (tid < SH) {
+      const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t, c);
+      sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
+    }
+  }
+  const bool has_p = a.p != nullptr;
+  if (has_p) {
+    for (int r = ty; r < PH; r += nty) {
+      const float* row = a.p + (size_t)((i0 - 3 + r) & M) * N;
+      for (int cc = tx; cc < PW; cc += 32) sP[r * PW + cc] = __ldg(row + ((j0 - 3 + cc) & M));
+    }
+  }
+  for (int r = ty; r < UH; r += nty) {
+    const size_t rowoff = (size_t)((i0 - 2 + r) & M) * N;
+    for (int cc = tx; cc < UW; cc += 32) {
+      const size_t g = rowoff + ((j0 - 2 + cc) & M);
+      sUx[r * UW + cc] = __ldg(a.us + g);
+      sUy[r * UW + cc] = __ldg(a.us + NN + g);
+    }
+  }
+  __syncthreads();
+
+  // 1. pending projection u^n = u* - dt * grad p
+  if (has_p) {
+    for (int r = ty; r < UH; r += nty) {
+      for (int cc = tx; cc < UW; cc += 32) {
+        const int op = (r + 1) * PW + (cc + 1);
+        const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
+        const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
+        const int ou = r * UW + cc;
+        sUx[ou] = fsub(sUx[ou], fmul(c.dt, px));
+        sUy[ou] = fsub(sUy[ou], fmul(c.dt, py));
+      }
+    }
+    __syncthreads();
+  }
+
+  // 2. objective partial on the state before the step; optional state output
+  float jacc = 0.0f;
+  for (int r = ty; r < TH; r += nty) {
+    for (int cc = tx; cc < TW; cc += 32) {
+      const int ou = (r + 2) * UW + (cc + 2);
+      if (MODE == MODE_ROLLOUT) jacc += sUx[ou] * sF[r + 1];
+      if (a.u_out) {
+        const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
+        a.u_out[g] = sUx[ou];
+        a.u_out[NN + g] = sUy[ou];
+      }
+    }
+  }
+
+  // 3. u*^{n+1} on the tile + 1 halo
+  for (int r = ty; r < SH; r += nty) {
+    for (int cc = tx; cc < SW; cc += 32) {
+      const int o = (r + 1) * UW + (cc + 1);
+      const float ux = sUx[o], uy = sUy[o];
+      const float lapx = lap5(sUx, o, UW, c), lapy = lap5(sUy, o, UW, c);
+      const float advx = adv5<SCHEME>(sUx, o, UW, ux, uy, c);
+      const float advy = adv5<SCHEME>(sUy, o, UW, ux, uy, c);
+      float fx, fy;
+      if (MODE == MODE_ROLLOUT) {
+        fx = sF[r];
+        fy = 0.0f;
+      } else {
+        const size_t g = (size_t)((i0 - 1 + r) & M) * N + ((j0 - 1 + cc) & M);
+        fx = __ldg(a.f + g);
+        fy = __ldg(a.f + NN + g);
+      }
+      sSx[r * SW + cc] = fadd(ux, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
+      sSy[r * SW + cc] = fadd(uy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+    }
+  }
+  __syncthreads();
+
+  // 4. write u*^{n+1} and div(u*^{n+1}) / dt
+  for (int r = ty; r < TH; r += nty) {
+    for (int cc = tx; cc < TW; cc += 32) {
+      const int o = (r + 1) * SW + (cc + 1);
+      const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
+      a.us_out[g] = sSx[o];
+      a.us_out[NN + g] = sSy[o];
+      const float gx = fdiv(fsub(sSx[o + SW], sSx[o - SW]), c.h2);
+      const float gy = fdiv(fsub(sSy[o + 1], sSy[o - 1]), c.h2);
+      a.rhs[g] = fdiv(fadd(gx, gy), c.dt);
+    }
+  }
+
+  if (MODE == MODE_ROLLOUT) {
+    jacc = warp_sum(jacc);
+    if (tx == 0) sRed[ty] = jacc;
+    __syncthreads();
+    if (ty == 0) {
+      float v = (tx < nty) ? sRed[tx] : 0.0f;
+      v = warp_sum(v);
+      if (tx == 0) {
+        const int nblk = gridDim.x * gridDim.y;
+        a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+      }
+    }
+  }
+}
+
+int stencil_nblocks(int N, int tw, int th) { return (N / tw) * (N / th); }
+
+static size_t stencil_smem(int tw, int th) {
+  const size_t f = (size_t)(th + 6) * (tw + 6) + 2 * (size_t)(th + 4) * (tw + 4) +
+                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 32;
+  return f * sizeof(float);
+}
+
+template <int SCHEME, int MODE>
+static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_stencil<SCHEME, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         160 * 1024);
+    configured = true;
+  }
+  const dim3 grid(a.c.N / a.tw, a.c.N / a.th);
+  k_stencil<SCHEME, MODE><<<grid, dim3(32, 8), stencil_smem(a.tw, a.th), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st) {
+  if (a.scheme == NSGB_SCHEME_CENTRAL) {
+    return mode == MODE_ROLLOUT ? launch_stencil_t<NSGB_SCHEME_CENTRAL, MODE_ROLLOUT>(a, st)
+                                : launch_stencil_t<NSGB_SCHEME_CENTRAL, MODE_FIELD>(a, st);
+  }
+  return mode == MODE_ROLLOUT ? launch_stencil_t<NSGB_SCHEME_UPWIND, MODE_ROLLOUT>(a, st)
+                              : launch_stencil_t<NSGB_SCHEME_UPWIND, MODE_FIELD>(a, st);
+}
+
+// ------------------------------------------------------------ projection --
+__global__ void k_project(const float* __restrict__ us, const float* __restrict__ p,
+                          float* __restrict__ u, const StepConsts c) {
+  const int N = c.N, M = N - 1;
+  const size_t NN = (size_t)N * N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  const int i = (int)(g >> c.logN), j = (int)(g & M);
+  const float px = fdiv(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
+                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2);
+  const float py = fdiv(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
+                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2);
+  u[g] = fsub(__ldg(us + g), fmul(c.dt, px));
+  u[NN + g] = fsub(__ldg(us + NN + g), fmul(c.dt, py));
+}
+
+cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
+                           cudaStream_t st) {
+  const size_t NN = (size_t)c.N * c.N;
+  k_project<<<(unsigned)((NN + 255) / 256), 256, 0, st>>>(us, p, u_out, c);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- J reduction --
+// One CTA per step: fixed-order sum of that step's block partials.
+__global__ void k_jreduce(const float* __restrict__ jpart, int nblk, double* __restrict__ jsteps) {
+  __shared__ double red[256];
+  const float* row = jpart + (size_t)blockIdx.x * nblk;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)row[b];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) jsteps[blockIdx.x] = red[0];
+}
+
+__global__ void k_jfinal(const double* __restrict__ jsteps, int steps, double jscale,
+                         float* __restrict__ J) {
+  double acc = 0.0;
+  for (int s = 0; s < steps; ++s) acc += jsteps[s] * jscale;
+  *J = (float)acc;
+}
+
+cudaError_t launch_jreduce(const float* jpart, int nblk, int steps, double* jsteps, float* J,
+                           double jscale, cudaStream_t st) {
+  if (steps > 0) k_jreduce<<<steps, 256, 0, st>>>(jpart, nblk, jsteps);
+  k_jfinal<<<1, 1, 0, st>>>(jsteps, steps, jscale, J);
+  return cudaGetLastError();
+}
+
+__global__ void k_step_counter(int* ctr, int value, int add) { *ctr = add ? *ctr + value : value; }
+cudaError_t launch_step_counter(int* step_ctr, int value, bool add, cudaStream_t st) {
+  k_step_counter<<<1, 1, 0, st>>>(step_ctr, value, add ? 1 : 0);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------- single operators --
+__device__ __forceinline__ void ij_of(size_t g, const StepConsts& c, int& i, int& j) {
+  i = (int)(g >> c.logN);
+  j = (int)(g & (c.N - 1));
+}
+
+__global__ void k_grad(const float* __restrict__ f, float* __restrict__ gx, float* __restrict__ gy,
+                       const StepConsts c) {
+  const size_t NN = (size_t)c.N * c.N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  int i, j;
+  ij_of(g, c, i, j);
+  const int N = c.N, M = N - 1;
+  gx[g] = fdiv(fsub(f[(size_t)((i + 1) & M) * N + j], f[(size_t)((i - 1) & M) * N + j]), c.h2);
+  gy[g] = fdiv(fsub(f[(size_t)i * N + ((j + 1) & M)], f[(size_t)i * N + ((j - 1) & M)]), c.h2);
+}
+
+__global__ void k_laplacian(const float* __restrict__ f, float* __restrict__ out, const StepConsts c) {
+  const size_t NN = (size_t)c.N * c.N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  int i, j;
+  ij_of(g, c, i, j);
+  const int N = c.N, M = N - 1;
+  const float left = f[(size_t)((i - 1) & M) * N + j], right = f[(size_t)((i + 1) & M) * N + j];
+  const float up = f[(size_t)i * N + ((j + 1) & M)], down = f[(size_t)i * N + ((j - 1) & M)];
+  out[g] = fdiv(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f[g])), c.dx2);
+}
+
+__global__ void k_divergence(const float* __restrict__ u, float* __restrict__ out, const StepConsts c) {
+  const size_t NN = (size_t)c.N * c.N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  int i, j;
+  ij_of(g, c, i, j);
+  const int N = c.N, M = N - 1;
+  const float* uy = u + NN;
+  const float gx = fdiv(fsub(u[(size_t)((i + 1) & M) * N + j], u[(size_t)((i - 1) & M) * N + j]), c.h2);
+  const float gy = fdiv(fsub(uy[(size_t)i * N + ((j + 1) & M)], uy[(size_t)i * N + ((j - 1) & M)]), c.h2);
+  out[g] = fadd(gx, gy);
+}
+
+template <int SCHEME>
+__global__ void k_advect(const float* __restrict__ fld, const float* __restrict__ ux,
+                         const float* __restrict__ uy, float* __restrict__ out, const StepConsts c) {
+  const size_t NN = (size_t)c.N * c.N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  int i, j;
+  ij_of(g, c, i, j);
+  const int N = c.N, M = N - 1;
+  const float f = fld[g];
+  const float left = fld[(size_t)((i - 1) & M) * N + j], right = fld[(size_t)((i + 1) & M) * N + j];
+  const float up = fld[(size_t)i * N + ((j + 1) & M)], down = fld[(size_t)i * N + ((j - 1) & M)];
+  const float vx = ux[g], vy = uy[g];
+  if (SCHEME == NSGB_SCHEME_CENTRAL) {
+    const float gx = fdiv(fsub(right, left), c.h2);
+    const float gy = fdiv(fsub(up, down), c.h2);
+    out[g] = -fadd(fmul(vx, gx), fmul(vy, gy));
+  } else {
+    const float dfx = fdiv(vx >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1);
+    const float dfy = fdiv(vy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1);
+    out[g] = -fadd(fmul(vx, dfx), fmul(vy, dfy));
+  }
+}
+
+__global__ void k_forcing_field(const float* __restrict__ theta, float t, float* __restrict__ f,
+                                const StepConsts c) {
+  const size_t NN = (size_t)c.N * c.N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  int i, j;
+  ij_of(g, c, i, j);
+  const ForcingRow fr = forcing_time(__ldg(theta), __ldg(theta + 1), t, c);
+  f[g] = forcing_fx(i, fr, c);
+  f[NN + g] = 0.0f;
+}
+
+static unsigned nb(const StepConsts& c) { return (unsigned)(((size_t)c.N * c.N + 255) / 256); }
+
+cudaError_t launch_grad(const float* f, float* gx, float* gy, const StepConsts& c, cudaStream_t st) {
+  k_grad<<<nb(c), 256, 0, st>>>(f, gx, gy, c);
+  return cudaGetLastError();
+}
+cudaError_t launch_laplacian(const float* f, float* out, const StepConsts& c, cudaStream_t st) {
+  k_laplacian<<<nb(c), 256, 0, st>>>(f, out, c);
+  return cudaGetLastError();
+}
+cudaError_t launch_divergence(const float* u, float* out, const StepConsts& c, cudaStream_t st) {
+  k_divergence<<<nb(c), 256, 0, st>>>(u, out, c);
+  return cudaGetLastError();
+}
+cudaError_t launch_advect(int scheme, const float* fld, const float* ux, const float* uy, float* out,
+                          const StepConsts& c, cudaStream_t st) {
+  if (scheme == NSGB_SCHEME_CENTRAL)
+    k_advect<NSGB_SCHEME_CENTRAL><<<nb(c), 256, 0, st>>>(fld, ux, uy, out, c);
+  else
+    k_advect<NSGB_SCHEME_UPWIND><<<nb(c), 256, 0, st>>>(fld, ux, uy, out, c);
+  return cudaGetLastError();
+}
+cudaError_t launch_forcing_field(const float* theta, int theta_len, float t, float* f,
+                                 const StepConsts& c, cudaStream_t st) {
+  (void)theta_len;
+  k_forcing_field<<<nb(c), 256, 0, st>>>(theta, t, f, c);
+  return cudaGetLastError();
+}
+
+}  // namespace nsgb

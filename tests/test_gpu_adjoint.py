@@ -1,0 +1,124 @@
+"""GPU parity of the hand-written discrete adjoint (jit_gradient / gradient /
+autograd through rollout) against the float64 autograd twin (stand-in for
+the reference's jax.grad), central finite differences of the GPU forward,
+and the reference's own JAX gradient recovered from its SGD trajectory."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import torch_twin as TT
+from ns_solver_jax_differential_distributed_gb300.workloads import spectral_u0
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nsgb(cuda_lib):
+    import ns_solver_jax_differential_distributed_gb300 as m
+    return m
+
+
+def make_solver(nsgb, N, L, nu, dt, steps, scheme, every=50):
+    grid = nsgb.make_grid(N, L)
+    phys = nsgb.Phys(nu=nu, mu0=0.5, sigma0=0.1, C=1.0)
+    return nsgb.SingleCoreNSSolver(grid, phys, nsgb.Time(dt=dt, steps=steps), scheme,
+                                   checkpoint_every=every)
+
+
+@pytest.mark.parametrize("scheme", ["central", "upwind"])
+@pytest.mark.parametrize("every", [1, 7, 50])
+def test_adjoint_vs_autograd_twin(nsgb, scheme, every):
+    """N=32, 24 steps, seeded u0, theta = [A, B, nu]: dJ/dtheta and dJ/du0
+    against float64 reverse-mode autograd, relative 1e-4 (float32 adjoint)."""
+    N, L, dt, steps = 32, 2 * math.pi, 1e-3, 24
+    u0 = spectral_u0(N, 8, 3)
+    th = np.array([0.9, 0.45, 2e-3], np.float32)
+    s = make_solver(nsgb, N, L, 2e-3, dt, steps, scheme, every)
+    J, g, du0 = s.gradient(torch.from_numpy(u0).cuda(), torch.from_numpy(th).cuda(), want_u0_grad=True)
+    Jt, gt, du0t = TT.gradient(u0.astype(np.float64), th.astype(np.float64), N, L, dt, steps, scheme,
+                               wrt_u0=True)
+    g = g.cpu().numpy().astype(np.float64)
+    assert abs(float(J) / Jt - 1) < 1e-4
+    for k in range(3):
+        assert abs(g[k] - gt[k]) <= 1e-4 * abs(gt[k]) + 1e-4 * np.abs(gt).max(), (k, g, gt)
+    du0 = du0.double().cpu().numpy()
+    assert np.linalg.norm(du0 - du0t) / np.linalg.norm(du0t) < 1e-4
+
+
+def test_checkpoint_interval_invariance(nsgb):
+    """The checkpoint interval changes memory, not results: bitwise equal."""
+    N, L = 64, 2 * math.pi
+    u0 = torch.from_numpy(spectral_u0(N, 8, 1)).cuda()
+    th = torch.tensor([1.1, 0.4, 1e-3]).cuda()
+    outs = [make_solver(nsgb, N, L, 1e-3, 1e-3, 30, "upwind", every).gradient(u0, th) for every in (1, 4, 30, 64)]
+    for J, g in outs[1:]:
+        assert torch.equal(J, outs[0][0]) and torch.equal(g, outs[0][1])
+
+
+@pytest.mark.parametrize("scheme", ["central", "upwind"])
+def test_adjoint_vs_finite_differences(nsgb, scheme):
+    """N=128, 200 steps, dt=1e-3, nu=1e-3: central differences of the GPU
+    forward with relative step 1e-3 per parameter."""
+    N, L, dt, steps = 128, 2 * math.pi, 1e-3, 200
+    u0 = torch.from_numpy(spectral_u0(N, 16, 0)).cuda()
+    th = np.array([1.05, 0.55, 1e-3], np.float64)
+    s = make_solver(nsgb, N, L, 1e-3, dt, steps, scheme, every=25)
+    _, g = s.gradient(u0, torch.tensor(th, dtype=torch.float32).cuda())
+    g = g.cpu().numpy().astype(np.float64)
+    fd = np.zeros(3)
+    for k in range(3):
+        h = 1e-3 * abs(th[k])
+        tp, tm = th.copy(), th.copy()
+        tp[k] += h
+        tm[k] -= h
+        Jp = s.rollout(u0, torch.tensor(tp, dtype=torch.float32).cuda())[0].double()
+        Jm = s.rollout(u0, torch.tensor(tm, dtype=torch.float32).cuda())[0].double()
+        fd[k] = float(Jp - Jm) / (2 * h)
+    # float32 forward differences carry ~1e-7 |J| / h noise; the rest is O(h^2)
+    for k in range(3):
+        assert abs(g[k] - fd[k]) <= 2e-3 * abs(fd[k]) + 2e-6, (k, g, fd)
+
+
+def test_reference_jax_gradient_golden(nsgb, golden):
+    """jit_gradient at theta0=[1, 0.5] of the reference's study configuration
+    (N=128, L=1, nu=0.01, 328 steps, zero IC) equals the JAX gradient that its
+    SGD(lr=0.1) trajectory recorded."""
+    sg = golden["studies"]["sgd"]
+    P = np.array(sg["parameters"])
+    g_ref = (P[0] - P[1]) / sg["lr"]
+    s = make_solver(nsgb, 128, 1.0, sg["nu"], sg["dt"], sg["steps"], "central")
+    g = s.jit_gradient(torch.tensor(P[0], dtype=torch.float32).cuda()).cpu().numpy()
+    assert abs(g[1] - g_ref[1]) < 2e-6 + 1e-5 * abs(g_ref[1])
+    assert abs(g[0] - g_ref[0]) < 2.5e-6
+    # and the objective the study recorded at theta_1
+    J1 = float(s.jit_objective(torch.tensor(P[1], dtype=torch.float32).cuda()))
+    assert abs(J1 / sg["objectives"][1] - 1) < 2e-6
+
+
+def test_autograd_function(nsgb):
+    """rollout() is differentiable through the adjoint when theta or u0
+    requires grad; the gradient equals gradient()."""
+    N, L = 32, 2 * math.pi
+    s = make_solver(nsgb, N, L, 1e-3, 1e-3, 16, "central", every=5)
+    u0 = torch.from_numpy(spectral_u0(N, 8, 2)).cuda().requires_grad_(True)
+    th = torch.tensor([0.95, 0.5, 1e-3], device="cuda", requires_grad=True)
+    J, uf = s.rollout(u0, th)
+    (3.0 * J).backward()
+    Jr, gr, du0 = s.gradient(u0.detach(), th.detach(), want_u0_grad=True)
+    assert torch.equal(J.detach(), Jr)
+    assert torch.allclose(th.grad, 3.0 * gr, rtol=1e-6, atol=0)
+    assert torch.allclose(u0.grad, 3.0 * du0, rtol=1e-6, atol=0)
+    assert not uf.requires_grad
+
+
+def test_two_entry_theta(nsgb):
+    """The reference's 2-entry theta: gradient has 2 entries, matches the
+    3-entry call's first two."""
+    N, L = 32, 1.0
+    s = make_solver(nsgb, N, L, 1e-2, 1e-3, 10, "upwind")
+    u0 = torch.from_numpy(spectral_u0(N, 4, 4)).cuda()
+    _, g2 = s.gradient(u0, torch.tensor([1.0, 0.5]).cuda())
+    _, g3 = s.gradient(u0, torch.tensor([1.0, 0.5, 1e-2]).cuda())
+    assert g2.shape == (2,) and torch.allclose(g2, g3[:2], rtol=1e-6, atol=0)
