@@ -153,6 +153,58 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
                       float* J, float* u_final, float* dJdtheta, float* dJdu0, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* One member of an ensemble of independent solves (see nsgb_ensemble_advance). */
+typedef struct nsgb_member {
+  const nsgb_plan* plan; /* plan of this member's N and L (tiles as tuned) */
+  nsgb_phys phys;
+  const float* u0;       /* (2,N,N) device; read when done_steps == 0 */
+  const float* theta;    /* device, theta_len entries */
+  int theta_len;
+  float* u_final;        /* (2,N,N) device; written when the member finishes */
+  float* J;              /* one float, device; written when the member finishes */
+  void* state;           /* device state kept between calls, at least
+                            nsgb_rollout_workspace_bytes(plan, total_steps) bytes,
+                            256-byte aligned; NULL: carved from the call's workspace */
+  int total_steps;       /* steps of the whole solve */
+  int done_steps;        /* steps already taken (0: start from u0) */
+} nsgb_member;
+
+/* Bytes of workspace for nsgb_ensemble_advance / nsgb_ensemble_rollout (the
+ * member table plus the state of every member whose `state` is NULL). */
+size_t nsgb_ensemble_workspace_bytes(const nsgb_member* members, int count);
+
+/* Ensemble form of SingleCoreNSSolver.rollout (NS_solver.py:732-750), used for
+ * batching and continuous batching: every member takes min(steps, total_steps
+ * - done_steps) further steps from its saved state; members that reach
+ * total_steps get u_final and J written.  Members with the same plan, scheme,
+ * progress parity and step count form a group, and each stage of a step is
+ * ONE batched launch per group (the member index is a grid dimension).  The
+ * results equal one nsgb_rollout per member bit for bit.  The caller advances
+ * done_steps itself. */
+int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* One-shot ensemble: all members start from u0 (done_steps ignored) and run
+ * total_steps (equal for all members).  Chunks of `chunk` steps (even; 0 =
+ * direct launches) are replayed as ONE CUDA graph per chunk in which the
+ * groups run as parallel branches; `workspace` must stay the same between
+ * calls for the cached graph to be reused. */
+int nsgb_ensemble_rollout(const nsgb_member* members, int count, int chunk, void* workspace,
+                          size_t workspace_bytes, void* stream);
+
+/* Measurement helper (no counterpart in the reference): runs the four kernels
+ * of one rollout step from state u0 `reps` times each on `stream`, each launch
+ * bracketed by CUDA events, and writes the mean device time per launch in
+ * milliseconds: out_ms[0] fused stencil, [1] row FFT forward, [2] column FFT
+ * with the Poisson multiplier, [3] row FFT inverse.  When flush != NULL,
+ * flush_bytes of it are overwritten before every timed launch (outside the
+ * events) so each launch starts with a cold L2.  Synchronises the stream.
+ * Workspace: nsgb_rollout_workspace_bytes(plan, 1). */
+int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
+                     const float* theta, int theta_len, int reps, void* flush,
+                     size_t flush_bytes, void* workspace, size_t workspace_bytes, float* out_ms,
+                     void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ SCHEME_IDS = {"central": 0, "upwind": 1}
 GRAD_FORWARD = 1
 GRAD_BACKWARD = 2
 
-_lock = threading.Lock()
+_lock = threading.RLock()
 _lib = None
 
 
@@ -29,6 +29,14 @@ class Phys(ctypes.Structure):
     _fields_ = [("L", ctypes.c_double), ("nu", ctypes.c_double), ("dt", ctypes.c_double),
                 ("mu0", ctypes.c_double), ("sigma0", ctypes.c_double), ("C", ctypes.c_double),
                 ("scheme", ctypes.c_int)]
+
+
+class Member(ctypes.Structure):
+    """``nsgb_member`` (include/nsgb.h): one solve of an ensemble."""
+    _fields_ = [("plan", ctypes.c_void_p), ("phys", Phys), ("u0", ctypes.c_void_p),
+                ("theta", ctypes.c_void_p), ("theta_len", ctypes.c_int), ("u_final", ctypes.c_void_p),
+                ("J", ctypes.c_void_p), ("state", ctypes.c_void_p), ("total_steps", ctypes.c_int),
+                ("done_steps", ctypes.c_int)]
 
 
 class NativeError(RuntimeError):
@@ -67,6 +75,10 @@ SIGNATURES = {
     "nsgb_step": ([_P, _PH, _P, _P, _I, _F, _P, _P, _S, _P], _I),
     "nsgb_rollout": ([_P, _PH, _P, _P, _I, _I, _P, _P, _P, _S, _I, _P], _I),
     "nsgb_rollout_grad": ([_P, _PH, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _S, _P], _I),
+    "nsgb_time_stages": ([_P, _PH, _P, _P, _I, _I, _P, _S, _P, _S, ctypes.POINTER(_F), _P], _I),
+    "nsgb_ensemble_workspace_bytes": ([ctypes.POINTER(Member), _I], _S),
+    "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
+    "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
 }
 
 
@@ -155,6 +167,7 @@ _plans: dict = {}
 
 
 def get_plan(N: int, L: float, device) -> Plan:
+    lib()  # load before taking the plan lock
     device = torch.device(device)
     if device.type != "cuda":
         raise RuntimeError(f"the GB300 solver runs on CUDA devices only, got {device}")
@@ -372,3 +385,27 @@ class GradSession:
              ptr(self.theta), self.theta.numel(), self.steps, self.every, GRAD_BACKWARD, None,
              None, ptr(g), ptr(du0), ptr(self.ws), self.ws.numel(), st)
         return g, du0
+
+
+STAGES = ("stencil", "rows_fwd", "cols", "rows_inv")
+# Algorithmic bytes per cell of each stage (float32): stencil reads u* (8) and
+# p (4) and writes u* (8) and rhs (4); each FFT pass reads and writes the
+# half spectrum or the real field once (4 + 4).
+STAGE_BYTES_PER_CELL = {"stencil": 24, "rows_fwd": 8, "cols": 8, "rows_inv": 8}
+
+
+def time_stages(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: float, scheme,
+                reps: int = 20, flush: torch.Tensor | None = None) -> dict:
+    """Mean device ms per launch of each stage kernel (CUDA events, cold L2
+    when `flush` is given)."""
+    u0, theta = _cuda_f32(u0, "u0"), _cuda_f32(theta, "theta")
+    N = _square(u0, "u0", 2)
+    p = get_plan(N, L, u0.device)
+    st = stream_of(u0.device)
+    ph = make_phys(L, nu, dt, scheme)
+    ws = p.workspace("time", lib().nsgb_rollout_workspace_bytes(p.handle, 1), st)
+    out = (_F * 4)()
+    call("nsgb_time_stages", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta), theta.numel(), int(reps),
+         ptr(flush), 0 if flush is None else flush.numel() * flush.element_size(), ptr(ws), ws.numel(),
+         out, st)
+    return dict(zip(STAGES, list(out)))

@@ -1,0 +1,119 @@
+"""Launch-shape autotuner for the solver kernels.
+
+For one (N, scheme, GPU) it times every valid candidate of each stage's launch
+shape with CUDA events (``nsgb_time_stages``: mean device time per launch,
+cold L2 for grids larger than L2) and keeps the fastest per stage:
+
+* stencil tile (width x height cells),
+* rows per CTA of the row FFTs (forward and inverse),
+* spectrum rows per CTA of the column FFT.
+
+Results are cached in a JSON file keyed by GPU name, N and scheme
+(``$NSGB_TUNE_CACHE`` or ``<package>/_autotune/tiles.json``) so a process
+tunes a size once.  The stages are independent kernels, so each shape is
+tuned separately.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import threading
+
+import torch
+
+from . import _native
+
+_CACHE_PATH = os.environ.get("NSGB_TUNE_CACHE") or os.path.join(
+    os.path.dirname(os.path.abspath(__file__)), "_autotune", "tiles.json")
+_lock = threading.Lock()
+
+STENCIL_TILES = [(32, 8), (64, 8), (64, 16), (128, 8), (32, 16), (64, 32), (128, 16), (32, 32)]
+ROW_CHOICES = [2, 4, 8, 16]
+COL_CHOICES = [1, 2, 4]
+
+
+def _load() -> dict:
+    try:
+        with open(_CACHE_PATH) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(data: dict) -> None:
+    os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
+    tmp = _CACHE_PATH + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, _CACHE_PATH)
+
+
+def _key(N: int, scheme: str, device) -> str:
+    return f"{torch.cuda.get_device_name(device)}|N={N}|{scheme}"
+
+
+def candidates(N: int) -> dict:
+    T = N // min(16, N)
+    st = [(w, h) for (w, h) in STENCIL_TILES if w <= N and h <= N]
+    rows = [r for r in ROW_CHOICES if r <= N and (r // 2) * T <= 1024]
+    cols = [c for c in COL_CHOICES if c <= N // 2 and c * T <= 512]
+    return {"stencil": st, "rows": rows, "cols": cols}
+
+
+def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, reps: int = 5,
+         force: bool = False, verbose: bool = False) -> dict:
+    """Tune and apply the launch shapes of the plan (N, L, device)."""
+    device = torch.device(device or "cuda")
+    plan = _native.get_plan(N, L, device)
+    key = _key(N, scheme, device)
+    with _lock:
+        cache = _load()
+        if key in cache and not force:
+            best = cache[key]
+            plan.set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
+            return best
+    from .workloads import spectral_u0
+    u0 = torch.from_numpy(spectral_u0(N, min(32, N // 4), 0)).to(device)
+    th = torch.tensor([1.0, 0.5, 1e-3], device=device)
+    dt, nu = 1e-4, 1e-3
+    cells = N * N
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device) if cells * 28 > (96 << 20) else None
+    cand = candidates(N)
+    base = plan.tiles()
+    results = {"stencil": {}, "rows": {}, "cols": {}}
+    for (w, h) in cand["stencil"]:
+        plan.set_tiles(w, h, base[2], base[3])
+        results["stencil"][(w, h)] = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)["stencil"]
+    for r in cand["rows"]:
+        plan.set_tiles(base[0], base[1], r, base[3])
+        t = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)
+        results["rows"][r] = t["rows_fwd"] + t["rows_inv"]
+    for c in cand["cols"]:
+        plan.set_tiles(base[0], base[1], base[2], c)
+        results["cols"][c] = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)["cols"]
+    tw, thh = min(results["stencil"], key=results["stencil"].get)
+    rows = min(results["rows"], key=results["rows"].get)
+    cols = min(results["cols"], key=results["cols"].get)
+    plan.set_tiles(tw, thh, rows, cols)
+    best = {"tw": tw, "th": thh, "rows": rows, "cols": cols,
+            "ms": {"stencil": results["stencil"][(tw, thh)], "rows_fwd+inv": results["rows"][rows],
+                   "cols": results["cols"][cols]},
+            "default": list(base)}
+    if verbose:
+        print(f"autotune N={N} {scheme}: {best}")
+    with _lock:
+        cache = _load()
+        cache[key] = best
+        _store(cache)
+    return best
+
+
+def apply_cached(N: int, L: float, scheme: str, device=None) -> bool:
+    """Apply cached shapes if present (no timing); True if applied."""
+    device = torch.device(device or "cuda")
+    best = _load().get(_key(N, scheme, device))
+    if not best:
+        return False
+    _native.get_plan(N, L, device).set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
+    return True

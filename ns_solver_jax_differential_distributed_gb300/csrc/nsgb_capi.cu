@@ -8,6 +8,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -241,6 +243,199 @@ int check_theta(const float* theta, int theta_len) {
   if (theta_len != 2 && theta_len != 3)
     return fail(NSGB_ERR_INVALID_ARG, "theta must have 2 or 3 entries, got %d", theta_len);
   return NSGB_OK;
+}
+
+
+// ------------------------------------------------------------- ensembles --
+// Variant of the argument set that performs step s of a member (see SolveDev).
+inline int variant_of(int s) { return s == 0 ? 0 : ((s & 1) ? 1 : 2); }
+
+struct EnsGroup {
+  const nsgb_plan* plan;
+  int scheme;
+  int first, count;  // range in the member table
+  int done, todo;    // progress of the group's first member (parity shared)
+};
+
+struct EnsLayout {
+  size_t tab_off = 0, fin_off = 0, bytes = 0;
+  std::vector<size_t> state_off;  // per member: offset of a carved state, or SIZE_MAX
+};
+
+EnsLayout ensemble_layout(const nsgb_member* m, int count) {
+  EnsLayout L;
+  size_t off = 0;
+  L.tab_off = off;
+  off += align_up(sizeof(SolveDev) * (size_t)count);
+  L.fin_off = off;
+  off += align_up(sizeof(SolveDev) * (size_t)count);
+  L.state_off.assign(count, (size_t)-1);
+  for (int k = 0; k < count; ++k) {
+    if (m[k].state) continue;
+    L.state_off[k] = off;
+    off += align_up(carve_rollout(m[k].plan, m[k].total_steps, nullptr).bytes);
+  }
+  L.bytes = off;
+  return L;
+}
+
+SolveDev make_solvedev(const nsgb_member& m, void* state) {
+  RolloutWs w = carve_rollout(m.plan, m.total_steps, state);
+  StencilArgs a = stencil_args(m.plan, &m.phys);
+  a.theta = m.theta;
+  a.theta_len = m.theta_len;
+  a.jpart = w.jpart;
+  a.rhs = w.rhs;
+  a.step_ctr = w.ctr;
+  a.step_fixed = 0;
+  a.t_from_step = 1;
+  SolveDev d;
+  d.st[0] = a;
+  d.st[0].us = m.u0;
+  d.st[0].p = nullptr;
+  d.st[0].us_out = w.usA;
+  d.st[1] = a;
+  d.st[1].us = w.usA;
+  d.st[1].p = w.p;
+  d.st[1].us_out = w.usB;
+  d.st[2] = a;
+  d.st[2].us = w.usB;
+  d.st[2].p = w.p;
+  d.st[2].us_out = w.usA;
+  d.fft = {w.rhs, (float2*)w.spec, w.p};
+  d.u_final = m.u_final;
+  d.J = m.J;
+  d.jsteps = w.jsteps;
+  const double dx = m.plan->L / m.plan->N;
+  d.jscale = m.phys.dt * dx * dx;
+  d.ctr = w.ctr;
+  d.ctr_init = m.done_steps;
+  return d;
+}
+
+int check_members(const nsgb_member* members, int count, bool need_state_size) {
+  if (!members || count <= 0) return fail(NSGB_ERR_INVALID_ARG, "empty ensemble");
+  for (int i = 0; i < count; ++i) {
+    const nsgb_member& m = members[i];
+    if (!m.plan) return fail(NSGB_ERR_INVALID_ARG, "member %d: plan is NULL", i);
+    if (int r = check_phys(&m.phys)) return r;
+    if (std::fabs(m.phys.L - m.plan->L) > 1e-12 * m.plan->L)
+      return fail(NSGB_ERR_INVALID_ARG, "member %d: phys.L differs from its plan's L", i);
+    if (int r = check_theta(m.theta, m.theta_len)) return r;
+    if (!m.u0 || !m.u_final || !m.J) return fail(NSGB_ERR_INVALID_ARG, "member %d: NULL pointer", i);
+    if (m.total_steps < 1) return fail(NSGB_ERR_INVALID_ARG, "member %d: total_steps must be >= 1", i);
+    if (m.done_steps < 0 || m.done_steps > m.total_steps)
+      return fail(NSGB_ERR_INVALID_ARG, "member %d: done_steps out of range", i);
+    if (m.state && ((uintptr_t)m.state & 255))
+      return fail(NSGB_ERR_WORKSPACE, "member %d: state must be 256-byte aligned", i);
+  }
+  (void)need_state_size;
+  return NSGB_OK;
+}
+
+struct EnsGraph {
+  const void* ws;
+  int count, chunk;
+  uint64_t sig;
+  cudaGraphExec_t exec;
+};
+std::mutex g_ens_mu;
+std::vector<EnsGraph> g_ens_graphs;
+cudaStream_t g_ens_streams[9] = {nullptr};
+cudaEvent_t g_ens_events[10] = {nullptr};
+
+uint64_t fnv(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
+  const unsigned char* c = (const unsigned char*)p;
+  for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  return h;
+}
+
+// One solver step (step `done + k`) of each group, on the group's stream.
+cudaError_t ensemble_step(const std::vector<EnsGroup>& groups, const SolveDev* dev, int k,
+                          const std::vector<cudaStream_t>& gs) {
+  for (size_t g = 0; g < groups.size(); ++g) {
+    const EnsGroup& G = groups[g];
+    if (k >= G.todo) continue;
+    const SolveDev* d = dev + G.first;
+    cudaStream_t st = gs[g % gs.size()];
+    cudaError_t e = launch_stencil_batch(d, G.count, variant_of(G.done + k), k, G.scheme, G.plan->N,
+                                         G.plan->tile_w, G.plan->tile_h, st);
+    if (e != cudaSuccess) return e;
+    e = poisson_fft_batch(G.plan->N, fft_launch(G.plan, nullptr, nullptr, nullptr), d, G.count, st);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Sort members into groups; fills `order` (table position -> member index).
+std::vector<EnsGroup> make_groups(const nsgb_member* m, int count, int steps, std::vector<int>& order) {
+  auto todo = [&](int i) { return std::min(steps, m[i].total_steps - m[i].done_steps); };
+  auto dk = [&](int i) { return m[i].done_steps == 0 ? 2 : (m[i].done_steps & 1); };
+  order.resize(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (m[a].plan->N != m[b].plan->N) return m[a].plan->N < m[b].plan->N;
+    if (m[a].plan != m[b].plan) return m[a].plan < m[b].plan;
+    if (m[a].phys.scheme != m[b].phys.scheme) return m[a].phys.scheme < m[b].phys.scheme;
+    if (dk(a) != dk(b)) return dk(a) < dk(b);
+    return todo(a) < todo(b);
+  });
+  std::vector<EnsGroup> groups;
+  for (int k = 0; k < count; ++k) {
+    const int i = order[k];
+    const nsgb_member& x = m[i];
+    bool same = !groups.empty();
+    if (same) {
+      const nsgb_member& y = m[order[groups.back().first]];
+      same = y.plan == x.plan && y.phys.scheme == x.phys.scheme && dk(order[groups.back().first]) == dk(i) &&
+             groups.back().todo == todo(i);
+    }
+    if (!same) groups.push_back({x.plan, x.phys.scheme, k, 0, x.done_steps, todo(i)});
+    groups.back().count++;
+  }
+  return groups;
+}
+
+// Final projection and objective of the members that finish in this call.
+cudaError_t ensemble_finalize(const nsgb_member* m, const std::vector<int>& order, const std::vector<SolveDev>& tab,
+                              int steps, SolveDev* fin_dev, cudaStream_t st) {
+  std::vector<int> fin;
+  for (size_t k = 0; k < order.size(); ++k) {
+    const nsgb_member& x = m[order[k]];
+    if (x.done_steps + std::min(steps, x.total_steps - x.done_steps) == x.total_steps) fin.push_back((int)k);
+  }
+  if (fin.empty()) return cudaSuccess;
+  std::stable_sort(fin.begin(), fin.end(), [&](int a, int b) {
+    const nsgb_member &x = m[order[a]], &y = m[order[b]];
+    if (x.plan != y.plan) return x.plan < y.plan;
+    if (variant_of(x.total_steps) != variant_of(y.total_steps))
+      return variant_of(x.total_steps) < variant_of(y.total_steps);
+    return x.total_steps < y.total_steps;
+  });
+  std::vector<SolveDev> ft(fin.size());
+  for (size_t k = 0; k < fin.size(); ++k) ft[k] = tab[fin[k]];
+  cudaError_t e = cudaMemcpyAsync(fin_dev, ft.data(), sizeof(SolveDev) * ft.size(), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  size_t a = 0;
+  while (a < fin.size()) {
+    const nsgb_member& x = m[order[fin[a]]];
+    size_t b = a + 1;
+    while (b < fin.size()) {
+      const nsgb_member& y = m[order[fin[b]]];
+      if (y.plan != x.plan || variant_of(y.total_steps) != variant_of(x.total_steps) ||
+          y.total_steps != x.total_steps)
+        break;
+      ++b;
+    }
+    const int n = (int)(b - a);
+    e = launch_project_batch(fin_dev + a, n, variant_of(x.total_steps), x.plan->N, st);
+    if (e == cudaSuccess)
+      e = launch_jreduce_batch(fin_dev + a, n, stencil_nblocks(x.plan->N, x.plan->tile_w, x.plan->tile_h),
+                               x.total_steps, st);
+    if (e != cudaSuccess) return e;
+    a = b;
+  }
+  return cudaSuccess;
 }
 
 // One forward step of a rollout: stencil (with the pending projection) then
@@ -667,6 +862,190 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
     NSGB_CUDA(launch_greduce(g.gpart, nblk, s1 - s0, g.gacc, st));
   }
   NSGB_CUDA(launch_gfinal(g.gacc, theta_len, dJdtheta, st));
+  return NSGB_OK;
+}
+
+size_t nsgb_ensemble_workspace_bytes(const nsgb_member* members, int count) {
+  if (!members || count <= 0) return 0;
+  for (int i = 0; i < count; ++i)
+    if (!members[i].plan || members[i].total_steps < 1) return 0;
+  return ensemble_layout(members, count).bytes;
+}
+
+int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void* workspace, size_t ws_bytes,
+                          void* stream) {
+  if (int r = check_members(members, count, true)) return r;
+  if (steps < 0) return fail(NSGB_ERR_INVALID_ARG, "steps must be >= 0");
+  EnsLayout L = ensemble_layout(members, count);
+  if (int r = check_ws(workspace, ws_bytes, L.bytes)) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = (char*)workspace;
+  SolveDev* dev = (SolveDev*)(base + L.tab_off);
+  std::vector<int> order;
+  std::vector<EnsGroup> groups = make_groups(members, count, steps, order);
+  std::vector<SolveDev> tab(count);
+  int maxtodo = 0;
+  for (int k = 0; k < count; ++k) {
+    const int i = order[k];
+    void* state = members[i].state ? members[i].state : (void*)(base + L.state_off[i]);
+    tab[k] = make_solvedev(members[i], state);
+  }
+  for (const EnsGroup& G : groups) maxtodo = std::max(maxtodo, G.todo);
+  NSGB_CUDA(cudaMemcpyAsync(dev, tab.data(), sizeof(SolveDev) * count, cudaMemcpyHostToDevice, st));
+  NSGB_CUDA(launch_counter_batch(dev, count, 0, false, st));  // counters = done_steps
+  std::vector<cudaStream_t> one{st};
+  for (int k = 0; k < maxtodo; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
+  NSGB_CUDA(ensemble_finalize(members, order, tab, steps, (SolveDev*)(base + L.fin_off), st));
+  return NSGB_OK;
+}
+
+int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, void* workspace, size_t ws_bytes,
+                          void* stream) {
+  if (int r = check_members(members_in, count, true)) return r;
+  if (chunk < 0 || (chunk % 2) != 0) return fail(NSGB_ERR_INVALID_ARG, "chunk must be even and >= 0");
+  const int steps = members_in[0].total_steps;
+  for (int i = 1; i < count; ++i)
+    if (members_in[i].total_steps != steps)
+      return fail(NSGB_ERR_INVALID_ARG, "nsgb_ensemble_rollout needs equal total_steps (use advance)");
+  std::vector<nsgb_member> members(members_in, members_in + count);
+  for (auto& m : members) m.done_steps = 0;
+  EnsLayout L = ensemble_layout(members.data(), count);
+  if (int r = check_ws(workspace, ws_bytes, L.bytes)) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = (char*)workspace;
+  SolveDev* dev = (SolveDev*)(base + L.tab_off);
+  std::vector<int> order;
+  std::vector<EnsGroup> groups = make_groups(members.data(), count, steps, order);
+  std::vector<SolveDev> tab(count);
+  for (int k = 0; k < count; ++k) {
+    const int i = order[k];
+    void* state = members[i].state ? members[i].state : (void*)(base + L.state_off[i]);
+    tab[k] = make_solvedev(members[i], state);
+  }
+  NSGB_CUDA(cudaMemcpyAsync(dev, tab.data(), sizeof(SolveDev) * count, cudaMemcpyHostToDevice, st));
+  NSGB_CUDA(launch_counter_batch(dev, count, 0, false, st));
+  std::vector<cudaStream_t> one{st};
+  // step 0 reads u0; then counters = 1 and the groups are at odd parity.
+  NSGB_CUDA(ensemble_step(groups, dev, 0, one));
+  NSGB_CUDA(launch_counter_batch(dev, count, 1, true, st));
+  for (auto& G : groups) {
+    G.done = 1;
+    G.todo = steps - 1;
+  }
+  int s = 1;
+  if (chunk > 0 && steps - 1 >= chunk) {
+    std::lock_guard<std::mutex> lk(g_ens_mu);
+    const uint64_t sig = fnv(tab.data(), sizeof(SolveDev) * count);
+    EnsGraph* eg = nullptr;
+    for (auto& g : g_ens_graphs)
+      if (g.ws == workspace && g.count == count && g.chunk == chunk && g.sig == sig) eg = &g;
+    if (!g_ens_streams[0]) {
+      for (auto& x : g_ens_streams) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      for (auto& x : g_ens_events) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+    }
+    cudaStream_t cs = g_ens_streams[0];
+    const int nbr = (int)std::min<size_t>(groups.size(), 8);
+    if (!eg) {
+      if (g_ens_graphs.size() >= 8) {
+        cudaGraphExecDestroy(g_ens_graphs.front().exec);
+        g_ens_graphs.erase(g_ens_graphs.begin());
+      }
+      std::vector<cudaStream_t> br(g_ens_streams + 1, g_ens_streams + 1 + nbr);
+      std::vector<EnsGroup> cg = groups;
+      for (auto& G : cg) G.todo = chunk;
+      cudaGraph_t graph;
+      NSGB_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      cudaError_t ce = cudaEventRecord(g_ens_events[0], cs);
+      for (int b = 0; b < nbr && ce == cudaSuccess; ++b) ce = cudaStreamWaitEvent(br[b], g_ens_events[0], 0);
+      for (int k = 0; k < chunk && ce == cudaSuccess; ++k) ce = ensemble_step(cg, dev, k, br);
+      for (int b = 0; b < nbr && ce == cudaSuccess; ++b) {
+        ce = cudaEventRecord(g_ens_events[1 + b], br[b]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, g_ens_events[1 + b], 0);
+      }
+      if (ce == cudaSuccess) ce = launch_counter_batch(dev, count, chunk, true, cs);
+      cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+      if (ce != cudaSuccess) return cuda_fail(ce, "ensemble graph capture");
+      if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
+      EnsGraph g{workspace, count, chunk, sig, nullptr};
+      cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
+      g_ens_graphs.push_back(g);
+      eg = &g_ens_graphs.back();
+    }
+    NSGB_CUDA(cudaEventRecord(g_ens_events[9], st));
+    NSGB_CUDA(cudaStreamWaitEvent(cs, g_ens_events[9], 0));
+    while (steps - s >= chunk) {
+      NSGB_CUDA(cudaGraphLaunch(eg->exec, cs));
+      s += chunk;
+    }
+    NSGB_CUDA(cudaEventRecord(g_ens_events[9], cs));
+    NSGB_CUDA(cudaStreamWaitEvent(st, g_ens_events[9], 0));
+  }
+  // remaining steps: the chunks kept the parity (chunk is even)
+  for (auto& G : groups) {
+    G.done = s;
+    G.todo = steps - s;
+  }
+  for (int k = 0; k < steps - s; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
+  NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + L.fin_off), st));
+  return NSGB_OK;
+}
+
+int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta,
+                     int theta_len, int reps, void* flush, size_t flush_bytes, void* workspace,
+                     size_t ws_bytes, float* out_ms, void* stream) {
+  if (int r = check_plan(plan)) return r;
+  if (int r = check_phys(phys)) return r;
+  if (int r = check_theta(theta, theta_len)) return r;
+  if (!u0 || !out_ms) return fail(NSGB_ERR_INVALID_ARG, "NULL pointer");
+  if (reps < 1) return fail(NSGB_ERR_INVALID_ARG, "reps must be >= 1");
+  const size_t need = carve_rollout(plan, 1, nullptr).bytes;
+  if (int r = check_ws(workspace, ws_bytes, need)) return r;
+  RolloutWs w = carve_rollout(plan, 1, workspace);
+  cudaStream_t st = (cudaStream_t)stream;
+  StencilArgs a = stencil_args(plan, phys);
+  a.theta = theta;
+  a.theta_len = theta_len;
+  // Steady state: one step from u0 leaves u* in usA and p pending.
+  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, true, st));
+  cudaEvent_t e0, e1;
+  NSGB_CUDA(cudaEventCreate(&e0));
+  NSGB_CUDA(cudaEventCreate(&e1));
+  double tot[4] = {0, 0, 0, 0};
+  cudaError_t err = cudaSuccess;
+  for (int stage = 0; stage < 4 && err == cudaSuccess; ++stage) {
+    for (int r = 0; r < reps && err == cudaSuccess; ++r) {
+      if (flush && flush_bytes) err = cudaMemsetAsync(flush, r & 0xff, flush_bytes, st);
+      if (err == cudaSuccess) err = cudaEventRecord(e0, st);
+      if (err != cudaSuccess) break;
+      if (stage == 0) {
+        StencilArgs b = a;
+        b.us = w.usA;
+        b.p = w.p;
+        b.us_out = w.usB;
+        b.rhs = w.rhs;
+        b.jpart = w.jpart;
+        b.step_fixed = 0;
+        err = launch_stencil(b, MODE_ROLLOUT, st);
+      } else {
+        FftLaunch L = fft_launch(plan, w.rhs, w.spec, w.p);
+        if (stage != 1) L.rhs = nullptr;
+        L.do_cols = (stage == 2);
+        if (stage != 3) L.p = nullptr;
+        err = poisson_fft(plan->N, L, st);
+      }
+      if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+      if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+      tot[stage] += ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return cuda_fail(err, "nsgb_time_stages");
+  for (int k = 0; k < 4; ++k) out_ms[k] = (float)(tot[k] / reps);
   return NSGB_OK;
 }
 

@@ -36,9 +36,8 @@ __host__ __device__ constexpr int pair_stride() {
 // ---------------------------------------------------------------- rows fwd --
 // blockDim = (T, P): P row pairs per CTA, rows [blockIdx.x * 2P, +2P).
 template <int N>
-__global__ void __launch_bounds__(1024) k_rows_fwd(const float* __restrict__ rhs,
-                                                   float2* __restrict__ spec,
-                                                   const float2* __restrict__ tw) {
+__device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, float2* __restrict__ spec,
+                                              const float2* __restrict__ tw) {
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
@@ -96,10 +95,8 @@ __device__ __forceinline__ float poisson_mult(float k2x, float k2y, float scale)
 
 // blockDim = (T, KB): KB spectrum rows per CTA, rows [blockIdx.x * KB, +KB).
 template <int N>
-__global__ void __launch_bounds__(512) k_cols(float2* __restrict__ spec,
-                                               const float2* __restrict__ tw,
-                                               const float* __restrict__ k2,
-                                               float scale) {
+__device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float2* __restrict__ tw,
+                                          const float* __restrict__ k2, float scale) {
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
@@ -164,9 +161,8 @@ __global__ void __launch_bounds__(512) k_cols(float2* __restrict__ spec,
 
 // ---------------------------------------------------------------- rows inv --
 template <int N>
-__global__ void __launch_bounds__(1024) k_rows_inv(const float2* __restrict__ spec,
-                                                   float* __restrict__ p,
-                                                   const float2* __restrict__ tw) {
+__device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, float* __restrict__ p,
+                                              const float2* __restrict__ tw) {
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
@@ -224,9 +220,44 @@ __global__ void __launch_bounds__(1024) k_rows_inv(const float2* __restrict__ sp
   }
 }
 
+// ---------------------------------------------------------------- kernels --
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_fwd(const float* __restrict__ rhs, float2* __restrict__ spec,
+                                                   const float2* __restrict__ tw) {
+  rows_fwd_body<N>(rhs, spec, tw);
+}
+template <int N>
+__global__ void __launch_bounds__(512) k_cols(float2* __restrict__ spec, const float2* __restrict__ tw,
+                                              const float* __restrict__ k2, float scale) {
+  cols_body<N>(spec, tw, k2, scale);
+}
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_inv(const float2* __restrict__ spec, float* __restrict__ p,
+                                                   const float2* __restrict__ tw) {
+  rows_inv_body<N>(spec, p, tw);
+}
+// Ensemble variants: blockIdx.y selects the member.
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_fwd_b(const SolveDev* __restrict__ sv,
+                                                     const float2* __restrict__ tw) {
+  const FftPtrs f = sv[blockIdx.y].fft;
+  rows_fwd_body<N>(f.rhs, f.spec, tw);
+}
+template <int N>
+__global__ void __launch_bounds__(512) k_cols_b(const SolveDev* __restrict__ sv, const float2* __restrict__ tw,
+                                                const float* __restrict__ k2, float scale) {
+  cols_body<N>(sv[blockIdx.y].fft.spec, tw, k2, scale);
+}
+template <int N>
+__global__ void __launch_bounds__(1024) k_rows_inv_b(const SolveDev* __restrict__ sv,
+                                                     const float2* __restrict__ tw) {
+  const FftPtrs f = sv[blockIdx.y].fft;
+  rows_inv_body<N>(f.spec, f.p, tw);
+}
+
 // ------------------------------------------------------------- launchers --
 template <int N>
-static cudaError_t launch_poisson_fft(const FftLaunch& L, cudaStream_t st) {
+static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
   constexpr int T = N / ept(N);
   const int P = L.rows_per_cta / 2;
   const int KB = L.cols_per_cta;
@@ -234,10 +265,21 @@ static cudaError_t launch_poisson_fft(const FftLaunch& L, cudaStream_t st) {
   const size_t smem_cols = (size_t)KB * pair_stride<N>() * sizeof(float);
   static bool configured = false;  // per-process attribute set-up (idempotent)
   if (!configured) {
-    cudaFuncSetAttribute(k_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    const int mx = 200 * 1024;
+    cudaFuncSetAttribute(k_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_rows_fwd_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_cols_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    cudaFuncSetAttribute(k_rows_inv_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
     configured = true;
+  }
+  if (sv) {
+    const dim3 gr(N / (2 * P), count), gc((N / 2) / KB, count);
+    k_rows_fwd_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
+    k_cols_b<N><<<gc, dim3(T, KB), smem_cols, st>>>(sv, L.tw, L.k2, L.scale);
+    k_rows_inv_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
+    return cudaGetLastError();
   }
   if (L.rhs) {
     k_rows_fwd<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.rhs, L.spec, L.tw);
@@ -258,19 +300,25 @@ size_t fft_cols_smem_bytes(int N, int cols_per_cta) {
   return (size_t)cols_per_cta * (2 * padlen(N) + 4) * sizeof(float);
 }
 
-cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st) {
+static cudaError_t dispatch(int N, const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
   switch (N) {
-    case 16: return launch_poisson_fft<16>(L, st);
-    case 32: return launch_poisson_fft<32>(L, st);
-    case 64: return launch_poisson_fft<64>(L, st);
-    case 128: return launch_poisson_fft<128>(L, st);
-    case 256: return launch_poisson_fft<256>(L, st);
-    case 512: return launch_poisson_fft<512>(L, st);
-    case 1024: return launch_poisson_fft<1024>(L, st);
-    case 2048: return launch_poisson_fft<2048>(L, st);
-    case 4096: return launch_poisson_fft<4096>(L, st);
+    case 16: return launch_poisson_fft<16>(L, sv, count, st);
+    case 32: return launch_poisson_fft<32>(L, sv, count, st);
+    case 64: return launch_poisson_fft<64>(L, sv, count, st);
+    case 128: return launch_poisson_fft<128>(L, sv, count, st);
+    case 256: return launch_poisson_fft<256>(L, sv, count, st);
+    case 512: return launch_poisson_fft<512>(L, sv, count, st);
+    case 1024: return launch_poisson_fft<1024>(L, sv, count, st);
+    case 2048: return launch_poisson_fft<2048>(L, sv, count, st);
+    case 4096: return launch_poisson_fft<4096>(L, sv, count, st);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st) { return dispatch(N, L, nullptr, 0, st); }
+
+cudaError_t poisson_fft_batch(int N, const FftLaunch& L, const SolveDev* solves, int count, cudaStream_t st) {
+  return dispatch(N, L, solves, count, st);
 }
 
 }  // namespace nsgb

@@ -51,6 +51,32 @@ struct StencilArgs {
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st);
 int stencil_nblocks(int N, int tw, int th);
 
+// ------------------------------------------------------------- ensembles --
+// Device-resident description of one member of an ensemble advanced by
+// batched launches (blockIdx.z / blockIdx.y = member).
+struct FftPtrs {
+  const float* rhs;
+  float2* spec;
+  float* p;
+};
+struct SolveDev {
+  StencilArgs st[3];  // 0: first step (u0 -> A), 1: A -> B, 2: B -> A
+  FftPtrs fft;
+  float* u_final;
+  float* J;
+  double* jsteps;
+  double jscale;
+  int* ctr;
+  int ctr_init;  // progress of the member when the call started
+};
+cudaError_t launch_stencil_batch(const SolveDev* solves, int count, int variant, int step_off, int scheme, int N,
+                                 int tw, int th, cudaStream_t st);
+cudaError_t launch_project_batch(const SolveDev* solves, int count, int variant, int N, cudaStream_t st);
+cudaError_t launch_jreduce_batch(const SolveDev* solves, int count, int nblk, int steps, cudaStream_t st);
+// add: *ctr += value; otherwise *ctr = ctr_init + value (per member)
+cudaError_t launch_counter_batch(const SolveDev* solves, int count, int value, bool add, cudaStream_t st);
+cudaError_t poisson_fft_batch(int N, const FftLaunch& L, const SolveDev* solves, int count, cudaStream_t st);
+
 // u_out = us - dt * grad(p)  (NS_solver.py:696-697)
 cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
                            cudaStream_t st);

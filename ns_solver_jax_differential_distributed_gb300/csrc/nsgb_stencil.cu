@@ -43,7 +43,7 @@ __device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, fl
 }
 
 template <int SCHEME, int MODE>
-__global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
+__device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off = 0) {
   extern __shared__ float sm[];
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
   int step = 0;
   float t = a.t_fixed;
   if (MODE == MODE_ROLLOUT) {
-    step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed;
+    step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
     if (a.t_from_step) t = fmul((float)step, c.dt);
   }
   const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
@@ -174,6 +174,18 @@ __global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
   }
 }
 
+template <int SCHEME, int MODE>
+__global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
+  stencil_body<SCHEME, MODE>(a);
+}
+
+// Ensemble variant: blockIdx.z selects the solve, `variant` its argument set.
+template <int SCHEME>
+__global__ void __launch_bounds__(256) k_stencil_batch(const SolveDev* __restrict__ solves, int variant,
+                                                      int step_off) {
+  stencil_body<SCHEME, MODE_ROLLOUT>(solves[blockIdx.z].st[variant], step_off);
+}
+
 int stencil_nblocks(int N, int tw, int th) { return (N / tw) * (N / th); }
 
 static size_t stencil_smem(int tw, int th) {
@@ -193,6 +205,26 @@ static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
   const dim3 grid(a.c.N / a.tw, a.c.N / a.th);
   k_stencil<SCHEME, MODE><<<grid, dim3(32, 8), stencil_smem(a.tw, a.th), st>>>(a);
   return cudaGetLastError();
+}
+
+template <int SCHEME>
+static cudaError_t launch_stencil_batch_t(const SolveDev* solves, int count, int variant, int step_off, int N,
+                                          int tw, int th, cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_stencil_batch<SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    configured = true;
+  }
+  const dim3 grid(N / tw, N / th, count);
+  k_stencil_batch<SCHEME><<<grid, dim3(32, 8), stencil_smem(tw, th), st>>>(solves, variant, step_off);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stencil_batch(const SolveDev* solves, int count, int variant, int step_off, int scheme, int N,
+                                 int tw, int th, cudaStream_t st) {
+  return scheme == NSGB_SCHEME_CENTRAL
+             ? launch_stencil_batch_t<NSGB_SCHEME_CENTRAL>(solves, count, variant, step_off, N, tw, th, st)
+             : launch_stencil_batch_t<NSGB_SCHEME_UPWIND>(solves, count, variant, step_off, N, tw, th, st);
 }
 
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st) {
@@ -227,6 +259,32 @@ cudaError_t launch_project(const float* us, const float* p, float* u_out, const 
   return cudaGetLastError();
 }
 
+__global__ void k_project_batch(const SolveDev* __restrict__ solves, int variant) {
+  const SolveDev& d = solves[blockIdx.y];
+  const StencilArgs& a = d.st[variant];
+  const StepConsts& c = a.c;
+  const int N = c.N, M = N - 1;
+  const size_t NN = (size_t)N * N;
+  const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= NN) return;
+  const int i = (int)(g >> c.logN), j = (int)(g & M);
+  const float* p = a.p;
+  const float px = fdiv(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
+                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2);
+  const float py = fdiv(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
+                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2);
+  d.u_final[g] = fsub(__ldg(a.us + g), fmul(c.dt, px));
+  d.u_final[NN + g] = fsub(__ldg(a.us + NN + g), fmul(c.dt, py));
+}
+
+// Projection of the final state of every solve: `variant` names the argument
+// set whose (us, p) hold the pending u* and pressure.
+cudaError_t launch_project_batch(const SolveDev* solves, int count, int variant, int N, cudaStream_t st) {
+  const size_t NN = (size_t)N * N;
+  k_project_batch<<<dim3((unsigned)((NN + 255) / 256), count), 256, 0, st>>>(solves, variant);
+  return cudaGetLastError();
+}
+
 // ----------------------------------------------------------- J reduction --
 // One CTA per step: fixed-order sum of that step's block partials.
 __global__ void k_jreduce(const float* __restrict__ jpart, int nblk, double* __restrict__ jsteps) {
@@ -254,6 +312,48 @@ cudaError_t launch_jreduce(const float* jpart, int nblk, int steps, double* jste
                            double jscale, cudaStream_t st) {
   if (steps > 0) k_jreduce<<<steps, 256, 0, st>>>(jpart, nblk, jsteps);
   k_jfinal<<<1, 1, 0, st>>>(jsteps, steps, jscale, J);
+  return cudaGetLastError();
+}
+
+__global__ void k_jreduce_batch(const SolveDev* __restrict__ solves, int nblk) {
+  __shared__ double red[256];
+  const SolveDev& d = solves[blockIdx.y];
+  const float* row = d.st[1].jpart + (size_t)blockIdx.x * nblk;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)row[b];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) d.jsteps[blockIdx.x] = red[0];
+}
+
+__global__ void k_jfinal_batch(const SolveDev* __restrict__ solves, int count, int steps) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const SolveDev& d = solves[k];
+  double acc = 0.0;
+  for (int s = 0; s < steps; ++s) acc += d.jsteps[s] * d.jscale;
+  *d.J = (float)acc;
+}
+
+cudaError_t launch_jreduce_batch(const SolveDev* solves, int count, int nblk, int steps, cudaStream_t st) {
+  if (steps > 0) k_jreduce_batch<<<dim3(steps, count), 256, 0, st>>>(solves, nblk);
+  k_jfinal_batch<<<(count + 127) / 128, 128, 0, st>>>(solves, count, steps);
+  return cudaGetLastError();
+}
+
+__global__ void k_counter_batch(const SolveDev* __restrict__ solves, int count, int value, int add) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  int* ctr = solves[k].ctr;
+  *ctr = add ? *ctr + value : solves[k].ctr_init + value;
+}
+
+cudaError_t launch_counter_batch(const SolveDev* solves, int count, int value, bool add, cudaStream_t st) {
+  k_counter_batch<<<(count + 127) / 128, 128, 0, st>>>(solves, count, value, add ? 1 : 0);
   return cudaGetLastError();
 }
 

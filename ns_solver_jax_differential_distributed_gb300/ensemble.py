@@ -1,0 +1,127 @@
+"""Ensembles of independent solves of uneven grid size, advanced together.
+
+``Ensemble.run()`` calls ``nsgb_ensemble_rollout``: members that share N and
+scheme form a group, every stage of a solver step is one batched launch per
+group, and chunks of steps replay as one CUDA graph in which the groups are
+parallel branches.  Each member's result equals its own plain
+``SingleCoreNSSolver.rollout`` (the per-member arithmetic and reduction order
+do not depend on the ensemble), which the tests check bit for bit.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _native, autotune
+
+
+Member = _native.Member
+
+
+def _bind():
+    return _native.lib()
+
+
+@dataclass
+class SolveSpec:
+    """One member: grid size, parameters and initial state."""
+    N: int
+    u0: np.ndarray
+    theta: np.ndarray
+    nu: float
+    dt: float
+    scheme: str = "central"
+    L: float = 2 * math.pi
+    mu0: float = 0.5
+    sigma0: float = 0.1
+    C: float = 1.0
+
+
+class Ensemble:
+    """Device-resident ensemble; ``run()`` advances all members by ``steps``."""
+
+    def __init__(self, specs, steps: int, device=None, chunk: int = 16, tune: bool = False):
+        self.device = torch.device(device or "cuda")
+        self.steps = int(steps)
+        self.chunk = int(chunk)
+        self.specs = list(specs)
+        if tune:
+            for N, scheme, L in sorted({(s.N, s.scheme, s.L) for s in self.specs}):
+                autotune.tune(N, L, scheme, self.device)
+        else:
+            for N, scheme, L in sorted({(s.N, s.scheme, s.L) for s in self.specs}):
+                autotune.apply_cached(N, L, scheme, self.device)
+        self.u0 = [torch.from_numpy(np.ascontiguousarray(s.u0, dtype=np.float32)).to(self.device)
+                   for s in self.specs]
+        self.theta = [torch.from_numpy(np.asarray(s.theta, dtype=np.float32)).to(self.device)
+                      for s in self.specs]
+        self.u_final = [torch.empty_like(u) for u in self.u0]
+        self.J = torch.empty(len(self.specs), dtype=torch.float32, device=self.device)
+        arr = (Member * len(self.specs))()
+        for k, s in enumerate(self.specs):
+            plan = _native.get_plan(s.N, s.L, self.device)
+            arr[k].plan = plan.handle.value
+            arr[k].phys = _native.make_phys(s.L, s.nu, s.dt, s.scheme, s.mu0, s.sigma0, s.C)
+            arr[k].u0 = self.u0[k].data_ptr()
+            arr[k].theta = self.theta[k].data_ptr()
+            arr[k].theta_len = self.theta[k].numel()
+            arr[k].u_final = self.u_final[k].data_ptr()
+            arr[k].J = self.J.data_ptr() + 4 * k
+            arr[k].state = None
+            arr[k].total_steps = self.steps
+            arr[k].done_steps = 0
+        self._members = arr
+        L = _bind()
+        nbytes = L.nsgb_ensemble_workspace_bytes(arr, len(self.specs))
+        if nbytes == 0:
+            raise ValueError("invalid ensemble")
+        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+
+    @property
+    def cell_steps(self) -> int:
+        return sum(s.N * s.N for s in self.specs) * self.steps
+
+    def run(self):
+        """Advance every member; returns (J[count], [u_final...])."""
+        L = _bind()
+        _native.check("nsgb_ensemble_rollout", L.nsgb_ensemble_rollout(
+            self._members, len(self.specs), self.chunk, self.workspace.data_ptr(),
+            self.workspace.numel(), _native.stream_of(self.device)))
+        return self.J, self.u_final
+
+    def run_advance(self, steps_per_call: int):
+        """The same ensemble through nsgb_ensemble_advance in slices of
+        ``steps_per_call`` steps (the continuous-batching entry point)."""
+        L = _bind()
+        done = 0
+        while True:
+            for k in range(len(self.specs)):
+                self._members[k].done_steps = done
+            _native.check("nsgb_ensemble_advance", L.nsgb_ensemble_advance(
+                self._members, len(self.specs), int(steps_per_call), self.workspace.data_ptr(),
+                self.workspace.numel(), _native.stream_of(self.device)))
+            done = min(self.steps, done + int(steps_per_call))
+            if done >= self.steps:
+                break
+        return self.J, self.u_final
+
+    def run_sequential(self):
+        """The same members as one plain rollout each (the comparison path)."""
+        Js, us = [], []
+        for s, u0, th in zip(self.specs, self.u0, self.theta):
+            J, u = _native.op_rollout(u0, th, self.steps, float(s.L), float(s.nu), float(s.dt),
+                                      _native.SCHEME_IDS[s.scheme], float(s.mu0), float(s.sigma0),
+                                      float(s.C), True)
+            Js.append(J)
+            us.append(u)
+        return torch.stack(Js), us
+
+
+def from_workload(members, scheme: str = "central"):
+    """SolveSpecs from ``workloads.ensemble()`` members."""
+    return [SolveSpec(N=m.N, u0=m.u0(), theta=m.theta, nu=m.nu, dt=m.dt, scheme=scheme, L=m.L)
+            for m in members]

@@ -1,0 +1,277 @@
+"""Serving loop: continuous batching of forward and gradient solves.
+
+Requests (N, steps, theta, u0, forward-only or forward+adjoint) arrive over
+time.  A scheduler thread owns the GPU:
+
+* admission -- a request is admitted (FIFO) when its device memory (state,
+  u0, outputs) fits the HBM budget and the active forward work stays under a
+  cap; it then keeps its fields resident on the device until it completes;
+* forward requests are continuously batched: each tick advances every
+  active forward request by up to ``slice_steps`` steps in one
+  ``nsgb_ensemble_advance`` call (one batched launch per stage per group of
+  equal N), so requests that arrive while others run join at the next tick;
+* gradient requests run ``nsgb_rollout_grad`` (forward with checkpoints +
+  discrete adjoint) on worker threads, each with its own CUDA stream, so
+  their kernels overlap the batched forward work on the device;
+* completion is detected with CUDA events; memory returns to the budget.
+
+Latency is measured from arrival to the moment the result (J, and dJ/dtheta
+for gradient requests) is on the host.  Results do not depend on what else
+is in flight: a request's arithmetic is that of a plain solve, which the
+tests check bit for bit.
+"""
+from __future__ import annotations
+
+import collections
+import math
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _native
+from .workloads import spectral_u0, theta_draw
+
+TWO_PI = 2.0 * math.pi
+
+
+@dataclass
+class Request:
+    rid: int
+    arrival: float          # seconds after the start of the trace
+    N: int
+    steps: int
+    kind: str               # "forward" or "grad"
+    seed: int
+    nu: float = 1e-3
+    dt: float = 1e-3
+    scheme: str = "central"
+    L: float = TWO_PI
+    theta: np.ndarray = None
+    # results
+    J: float = None
+    grad: np.ndarray = None
+    u_final: torch.Tensor = field(default=None, repr=False)
+    t_admit: float = None
+    t_done: float = None
+
+    @property
+    def cells(self) -> int:
+        return self.N * self.N * self.steps
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def make_trace(rate: float = 200.0, duration: float = 60.0, seed: int = 7,
+               sizes=(128, 256, 512, 1024, 2048), steps_range=(100, 2000), p_grad: float = 0.3,
+               dt: float = 1e-3, nu_default: float = 1e-3):
+    """Poisson arrivals; N uniform over `sizes` (log-uniform over the
+    power-of-two set), steps uniform in `steps_range`, gradient with
+    probability `p_grad`; theta seeded per request."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        rid = len(out)
+        N = int(rng.choice(np.asarray(sizes)))
+        steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
+        kind = "grad" if rng.random() < p_grad else "forward"
+        th = theta_draw(nu_default, seed=rid)
+        out.append(Request(rid, t, N, steps, kind, rid, nu=float(th[2]), dt=dt, theta=th))
+    return out
+
+
+class _U0Cache:
+    """Seeded initial states; requests share 16 seeds per N (the generator
+    costs far more host time than a request's arrival interval at N=2048)."""
+
+    def __init__(self, device, K=32, variants=16):
+        self.device, self.K, self.variants = device, K, variants
+        self._c = {}
+
+    def get(self, N: int, seed: int) -> torch.Tensor:
+        key = (N, seed % self.variants)
+        if key not in self._c:
+            self._c[key] = torch.from_numpy(spectral_u0(N, min(self.K, N // 4), key[1])).to(self.device)
+        return self._c[key]
+
+
+class Server:
+    def __init__(self, device=None, hbm_budget: float = 150e9, slice_steps: int = 32,
+                 max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 4):
+        self.device = torch.device(device or "cuda")
+        self.budget = float(hbm_budget)
+        self.slice = int(slice_steps)
+        self.max_active_cells = float(max_active_cells)
+        self.grad_workers = int(grad_workers)
+        self.u0 = _U0Cache(self.device)
+        self.used = 0.0
+        self.stats = collections.Counter()
+        self._lock = threading.Lock()
+
+    # -- memory accounting
+    def _fwd_bytes(self, r: Request) -> int:
+        plan = _native.get_plan(r.N, r.L, self.device)
+        st = _native.lib().nsgb_rollout_workspace_bytes(plan.handle, r.steps)
+        return int(st + 8 * r.N * r.N + 4096)  # state + u_final
+
+    def _grad_bytes(self, r: Request) -> int:
+        plan = _native.get_plan(r.N, r.L, self.device)
+        return int(_native.lib().nsgb_rollout_grad_workspace_bytes(plan.handle, r.steps, 50) + 4096)
+
+    # -- gradient workers
+    def _grad_worker(self, q: "queue.Queue", done_q: "queue.Queue"):
+        torch.cuda.set_device(self.device)
+        stream = torch.cuda.Stream(self.device)
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            r, nbytes = item
+            with torch.cuda.stream(stream):
+                u0 = self.u0.get(r.N, r.seed)
+                th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
+                J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
+                                                      want_u_final=False)
+                Jh, gh = J.to("cpu", non_blocking=True), g.to("cpu", non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+            ev.synchronize()
+            r.J, r.grad = float(Jh), gh.numpy().copy()
+            done_q.put((r, nbytes))
+
+    def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None):
+        """Serve `requests` (sorted by arrival).  With realtime, arrivals
+        follow the wall clock; otherwise all are available at once.  Stops
+        when all are done or `drain_limit` seconds after the last arrival."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        pending = collections.deque()
+        nxt = 0
+        active = []          # forward requests: dict(r, state, done, out, J)
+        grad_q, grad_done = queue.Queue(), queue.Queue()
+        workers = [threading.Thread(target=self._grad_worker, args=(grad_q, grad_done), daemon=True)
+                   for _ in range(self.grad_workers)]
+        for w in workers:
+            w.start()
+        grads_inflight = 0
+        finishing = []       # (event, r, nbytes, J tensor)
+        last_arrival = reqs[-1].arrival if reqs else 0.0
+        t0 = time.perf_counter() if t0 is None else t0
+        L = _native.lib()
+        ws = None
+        stream = torch.cuda.current_stream(self.device)
+        completed = []
+        queue_trace = []
+        while True:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and (not realtime or reqs[nxt].arrival <= now):
+                pending.append(reqs[nxt])
+                nxt += 1
+            # admission (FIFO): memory budget, and a cap on active forward work
+            act_cells = sum(a["r"].N ** 2 for a in active)
+            while pending:
+                r = pending[0]
+                nb = self._grad_bytes(r) if r.kind == "grad" else self._fwd_bytes(r)
+                if self.used + nb > self.budget:
+                    break
+                if r.kind == "forward" and act_cells + r.N ** 2 > self.max_active_cells and active:
+                    break
+                if r.kind == "grad" and grads_inflight >= 2 * self.grad_workers:
+                    break
+                pending.popleft()
+                self.used += nb
+                r.t_admit = time.perf_counter() - t0
+                if r.kind == "grad":
+                    grads_inflight += 1
+                    grad_q.put((r, nb))
+                else:
+                    plan = _native.get_plan(r.N, r.L, self.device)
+                    st_bytes = L.nsgb_rollout_workspace_bytes(plan.handle, r.steps)
+                    state = torch.empty(st_bytes, dtype=torch.uint8, device=self.device)
+                    out = torch.empty((2, r.N, r.N), dtype=torch.float32, device=self.device)
+                    Jt = torch.empty((), dtype=torch.float32, device=self.device)
+                    th = torch.from_numpy(r.theta).to(self.device)
+                    active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=0, nb=nb, plan=plan))
+                    act_cells += r.N ** 2
+            # one tick of continuous batching over the active forward requests
+            if active:
+                arr = (_native.Member * len(active))()
+                for k, a in enumerate(active):
+                    r = a["r"]
+                    arr[k].plan = a["plan"].handle.value
+                    arr[k].phys = _native.make_phys(r.L, r.nu, r.dt, r.scheme)
+                    arr[k].u0 = self.u0.get(r.N, r.seed).data_ptr()
+                    arr[k].theta = a["th"].data_ptr()
+                    arr[k].theta_len = a["th"].numel()
+                    arr[k].u_final = a["out"].data_ptr()
+                    arr[k].J = a["J"].data_ptr()
+                    arr[k].state = a["state"].data_ptr()
+                    arr[k].total_steps = r.steps
+                    arr[k].done_steps = a["done"]
+                need = L.nsgb_ensemble_workspace_bytes(arr, len(active))
+                if ws is None or ws.numel() < need:
+                    ws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
+                _native.check("nsgb_ensemble_advance", L.nsgb_ensemble_advance(
+                    arr, len(active), self.slice, ws.data_ptr(), ws.numel(), stream.cuda_stream))
+                keep = []
+                for a in active:
+                    a["done"] = min(a["r"].steps, a["done"] + self.slice)
+                    if a["done"] >= a["r"].steps:
+                        ev = torch.cuda.Event()
+                        ev.record(stream)
+                        finishing.append((ev, a))
+                    else:
+                        keep.append(a)
+                active = keep
+                self.stats["ticks"] += 1
+            # completions
+            still = []
+            for ev, a in finishing:
+                if ev.query():
+                    r = a["r"]
+                    r.J = float(a["J"])
+                    r.u_final = a["out"]
+                    r.t_done = time.perf_counter() - t0
+                    self.used -= a["nb"]
+                    completed.append(r)
+                else:
+                    still.append((ev, a))
+            finishing = still
+            while not grad_done.empty():
+                r, nb = grad_done.get()
+                r.t_done = time.perf_counter() - t0
+                self.used -= nb
+                grads_inflight -= 1
+                completed.append(r)
+            queue_trace.append((now, len(pending), len(active), grads_inflight))
+            all_in = nxt >= len(reqs)
+            if all_in and not pending and not active and not finishing and grads_inflight == 0:
+                break
+            if drain_limit is not None and now > last_arrival + drain_limit:
+                break
+            if not active and not finishing:
+                time.sleep(0.0005)
+        for _ in workers:
+            grad_q.put(None)
+        torch.cuda.synchronize(self.device)
+        return completed, queue_trace
+
+
+def summarize(requests, completed, wall: float) -> dict:
+    lat = np.array([r.latency for r in completed if r.latency is not None])
+    cells = sum(r.cells * (3.5 if r.kind == "grad" else 1.0) for r in completed)
+    return {
+        "offered": len(requests), "completed": len(completed),
+        "solves_per_s": len(completed) / wall if wall > 0 else 0.0,
+        "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
+        "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
+        "forward_equiv_cell_steps_per_s": cells / wall if wall > 0 else 0.0,
+        "wall_s": wall,
+    }

@@ -33,7 +33,7 @@ import numpy as np
 __all__ = [
     "OracleConfig", "grid_x", "poisson_inv_k2", "forcing_fx", "grad", "laplacian",
     "divergence", "upwind_advect", "central_advect", "poisson_solve",
-    "projector_step", "solver_step", "rollout", "objective", "fd_gradient",
+    "projector_step", "solver_step", "rollout", "objective", "fd_gradient", "set_fft_workers",
 ]
 
 
@@ -166,6 +166,30 @@ def advect(f, ux, uy, dx, scheme: str):
 
 
 # ----------------------------------------------------------------- Poisson --
+_FFT_WORKERS = None
+
+
+def set_fft_workers(n):
+    """Run the oracle's FFTs with scipy.fft on n threads (None: numpy.fft).
+    Both keep complex64 for float32 input; used by the timed CPU baseline."""
+    global _FFT_WORKERS
+    _FFT_WORKERS = n
+
+
+def _fft2(x):
+    if _FFT_WORKERS:
+        import scipy.fft
+        return scipy.fft.fft2(x, workers=_FFT_WORKERS)
+    return np.fft.fft2(x)
+
+
+def _ifft2(x):
+    if _FFT_WORKERS:
+        import scipy.fft
+        return scipy.fft.ifft2(x, workers=_FFT_WORKERS)
+    return np.fft.ifft2(x)
+
+
 def poisson_solve(rhs: np.ndarray, dx: float, inv_k2: np.ndarray | None = None) -> np.ndarray:
     """p = Re ifft2(-fft2(rhs) * inv_k2) with p_hat[0,0] = 0 (NS_solver.py:523-527).
 
@@ -176,10 +200,10 @@ def poisson_solve(rhs: np.ndarray, dx: float, inv_k2: np.ndarray | None = None) 
     if inv_k2 is None:
         inv_k2 = poisson_inv_k2(N, dx, rhs.dtype.type)
     ctype = np.complex64 if rhs.dtype == np.float32 else np.complex128
-    F = np.fft.fft2(rhs.astype(ctype))
+    F = _fft2(rhs.astype(ctype))
     p_hat = (-F * inv_k2).astype(ctype)
     p_hat[0, 0] = 0.0
-    return np.fft.ifft2(p_hat).real.astype(rhs.dtype)
+    return _ifft2(p_hat).real.astype(rhs.dtype)
 
 
 # ---------------------------------------------------------- time stepping --

@@ -59,26 +59,24 @@ def test_checkpoint_interval_invariance(nsgb):
 
 @pytest.mark.parametrize("scheme", ["central", "upwind"])
 def test_adjoint_vs_finite_differences(nsgb, scheme):
-    """N=128, 200 steps, dt=1e-3, nu=1e-3: central differences of the GPU
-    forward with relative step 1e-3 per parameter."""
-    N, L, dt, steps = 128, 2 * math.pi, 1e-3, 200
-    u0 = torch.from_numpy(spectral_u0(N, 16, 0)).cuda()
+    """N=64, 100 steps, dt=1e-3: central finite differences of the float64
+    oracle.  Relative steps: 1e-3 for B and nu; 1e-4 for A, because the
+    reference's forcing wraps its Gaussian with period 1 (round, NS_solver.py:626)
+    and with sigma up to 1.1 the profile has kinks at d = +-1/2 that an A-step
+    of 1e-3 straddles (FD then misses by ~1% even in float64)."""
+    from oracle import ns_oracle as O
+    N, L, dt, steps = 64, 2 * math.pi, 1e-3, 100
+    u0 = spectral_u0(N, 16, 0)
     th = np.array([1.05, 0.55, 1e-3], np.float64)
     s = make_solver(nsgb, N, L, 1e-3, dt, steps, scheme, every=25)
-    _, g = s.gradient(u0, torch.tensor(th, dtype=torch.float32).cuda())
+    _, g = s.gradient(torch.from_numpy(u0).cuda(), torch.tensor(th, dtype=torch.float32).cuda())
     g = g.cpu().numpy().astype(np.float64)
-    fd = np.zeros(3)
+    cfg = O.OracleConfig(N=N, L=L, nu=1e-3, dt=dt, steps=steps, scheme=scheme)
+    fn = lambda t_: O.rollout(u0.astype(np.float64), t_, cfg)[0]
+    fd = np.array([O.fd_gradient(fn, th, rs)[k] for k, rs in enumerate((1e-4, 1e-3, 1e-3))])
+    tol = (2e-4, 2e-4, 3e-3)
     for k in range(3):
-        h = 1e-3 * abs(th[k])
-        tp, tm = th.copy(), th.copy()
-        tp[k] += h
-        tm[k] -= h
-        Jp = s.rollout(u0, torch.tensor(tp, dtype=torch.float32).cuda())[0].double()
-        Jm = s.rollout(u0, torch.tensor(tm, dtype=torch.float32).cuda())[0].double()
-        fd[k] = float(Jp - Jm) / (2 * h)
-    # float32 forward differences carry ~1e-7 |J| / h noise; the rest is O(h^2)
-    for k in range(3):
-        assert abs(g[k] - fd[k]) <= 2e-3 * abs(fd[k]) + 2e-6, (k, g, fd)
+        assert abs(g[k] - fd[k]) <= tol[k] * abs(fd[k]), (k, g, fd)
 
 
 def test_reference_jax_gradient_golden(nsgb, golden):
