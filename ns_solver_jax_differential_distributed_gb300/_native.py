@@ -334,15 +334,20 @@ def op_rollout(u0: torch.Tensor, theta: torch.Tensor, steps: int, L: float, nu: 
 
 def rollout_grad_raw(u0: torch.Tensor, theta: torch.Tensor, steps: int, every: int, L: float,
                      nu: float, dt: float, scheme, mu0=0.5, sigma0=0.1, C=1.0,
-                     want_u_final: bool = True, want_du0: bool = False):
-    """Forward + adjoint in one call: returns (J, dJ/dtheta, u_final, dJ/du0)."""
+                     want_u_final: bool = True, want_du0: bool = False, own_workspace: bool = False):
+    """Forward + adjoint in one call: returns (J, dJ/dtheta, u_final, dJ/du0).
+    With own_workspace the scratch is allocated for this call only (freed when
+    the call's tensors are), instead of the plan's cached workspace."""
     u0, theta = _cuda_f32(u0, "u0"), _cuda_f32(theta, "theta")
     N = _square(u0, "u0", 2)
     p = get_plan(N, L, u0.device)
     st = stream_of(u0.device)
     ph = make_phys(L, nu, dt, scheme, mu0, sigma0, C)
     nbytes = lib().nsgb_rollout_grad_workspace_bytes(p.handle, int(steps), int(every))
-    ws = p.workspace("grad", nbytes, st)
+    if own_workspace:
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=u0.device)
+    else:
+        ws = p.workspace("grad", nbytes, st)
     J = torch.empty((), dtype=torch.float32, device=u0.device)
     g = torch.empty(theta.numel(), dtype=torch.float32, device=u0.device)
     uf = torch.empty_like(u0) if want_u_final else None

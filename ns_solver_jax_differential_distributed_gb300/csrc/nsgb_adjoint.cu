@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   float* sF = sLy + SH * SW;   // fx for the SH rows of the lambda tile
   float* sDA = sF + SH;        // dfx/dA for the TH interior rows
   float* sDB = sDA + TH;       // dfx/dB
-  float* sRed = sDB + TH;      // 3 x 8
+  double* sRed = reinterpret_cast<double*>(sDB + TH + ((TH & 1) ? 1 : 0));  // 3 x 8 doubles
 
   const float dt = c.dt;
   const float jscale = c.jscale;  // float32(dt * dx^2) = dJ/du_x / f_x
@@ -109,17 +109,18 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     __syncthreads();
   }
 
-  // theta sensitivities on the interior cells
-  float gA = 0.f, gB = 0.f, gN = 0.f;
+  // theta sensitivities on the interior cells, accumulated in double: the
+  // nu term is a small difference of large contributions
+  double gA = 0.0, gB = 0.0, gN = 0.0;
   for (int r = ty; r < TH; r += nty) {
     for (int cc = tx; cc < TW; cc += 32) {
       const int o = (r + 2) * UW + (cc + 2);
       const float w = jscale * sUx[o] + dt * sMx[o];
-      gA += w * sDA[r];
-      gB += w * sDB[r];
+      gA += (double)(w * sDA[r]);
+      gB += (double)(w * sDB[r]);
       const float lux = (sUx[o - UW] + sUx[o + UW] + sUx[o + 1] + sUx[o - 1] - 4.0f * sUx[o]) / c.dx2;
       const float luy = (sUy[o - UW] + sUy[o + UW] + sUy[o + 1] + sUy[o - 1] - 4.0f * sUy[o]) / c.dx2;
-      gN += dt * (sMx[o] * lux + sMy[o] * luy);
+      gN += (double)dt * ((double)sMx[o] * lux + (double)sMy[o] * luy);
     }
   }
 
@@ -183,9 +184,9 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     }
   }
 
-  gA = warp_sum(gA);
-  gB = warp_sum(gB);
-  gN = warp_sum(gN);
+  gA = warp_sum_d(gA);
+  gB = warp_sum_d(gB);
+  gN = warp_sum_d(gN);
   if (tx == 0) {
     sRed[ty] = gA;
     sRed[8 + ty] = gB;
@@ -193,15 +194,15 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
   __syncthreads();
   if (ty == 0) {
-    float v0 = (tx < nty) ? sRed[tx] : 0.f;
-    float v1 = (tx < nty) ? sRed[8 + tx] : 0.f;
-    float v2 = (tx < nty) ? sRed[16 + tx] : 0.f;
-    v0 = warp_sum(v0);
-    v1 = warp_sum(v1);
-    v2 = warp_sum(v2);
+    double v0 = (tx < nty) ? sRed[tx] : 0.0;
+    double v1 = (tx < nty) ? sRed[8 + tx] : 0.0;
+    double v2 = (tx < nty) ? sRed[16 + tx] : 0.0;
+    v0 = warp_sum_d(v0);
+    v1 = warp_sum_d(v1);
+    v2 = warp_sum_d(v2);
     if (tx == 0) {
       const int nblk = gridDim.x * gridDim.y;
-      float* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
+      double* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
       gp[0] = v0;
       gp[1] = v1;
       gp[2] = v2;
@@ -210,9 +211,10 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
 }
 
 static size_t adjoint_smem(int tw, int th) {
+  // floats of the tiles and forcing rows, then 24 doubles (8-byte aligned)
   const size_t f = (size_t)(th + 6) * (tw + 6) + 4 * (size_t)(th + 4) * (tw + 4) +
-                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 2 * th + 24;
-  return f * sizeof(float);
+                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 2 * th + 2;
+  return f * sizeof(float) + 24 * sizeof(double) + 8;
 }
 
 template <int SCHEME>
@@ -233,11 +235,11 @@ cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
 }
 
 // Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double).
-__global__ void k_greduce(const float* __restrict__ gpart, int nblk, int nrows,
+__global__ void k_greduce(const double* __restrict__ gpart, int nblk, int nrows,
                           double* __restrict__ gacc) {
   __shared__ double red[3][256];
   for (int row = 0; row < nrows; ++row) {
-    const float* base = gpart + (size_t)row * nblk * 3;
+    const double* base = gpart + (size_t)row * nblk * 3;
     double v0 = 0, v1 = 0, v2 = 0;
     for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
       v0 += base[3 * b];
@@ -265,7 +267,7 @@ __global__ void k_greduce(const float* __restrict__ gpart, int nblk, int nrows,
   }
 }
 
-cudaError_t launch_greduce(const float* gpart, int nblk, int nrows, double* gacc, cudaStream_t st) {
+cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st) {
   if (nrows > 0) k_greduce<<<1, 256, 0, st>>>(gpart, nblk, nrows, gacc);
   return cudaGetLastError();
 }

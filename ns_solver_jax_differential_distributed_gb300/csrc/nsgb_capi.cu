@@ -52,6 +52,7 @@ size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct GraphEntry {
   const void* ws = nullptr;
+  int steps = 0;
   const float* theta = nullptr;
   int theta_len = 0;
   int chunk = 0;
@@ -185,6 +186,7 @@ struct RolloutWs {
   float *usA, *usB, *p, *rhs, *spec, *jpart;
   double* jsteps;
   int* ctr;
+  int steps;  // rows of jpart
   size_t bytes;
 };
 
@@ -193,6 +195,9 @@ RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
   const int nblk = stencil_nblocks(plan->N, plan->tile_w, plan->tile_h);
   Carver cv(ws);
   RolloutWs w;
+  // Buffers that captured graphs reference come first, at offsets that do
+  // not depend on `steps`.
+  w.ctr = cv.take<int>(1);
   w.usA = cv.take<float>(2 * NN);
   w.usB = cv.take<float>(2 * NN);
   w.p = cv.take<float>(NN);
@@ -200,15 +205,15 @@ RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
   w.spec = cv.take<float>(NN);
   w.jpart = cv.take<float>((size_t)(steps > 0 ? steps : 1) * nblk);
   w.jsteps = cv.take<double>(steps > 0 ? steps : 1);
-  w.ctr = cv.take<int>(1);
+  w.steps = steps > 0 ? steps : 1;
   w.bytes = cv.off;
   return w;
 }
 
 struct GradWs {
   RolloutWs f;
-  float *ckpt, *ustore, *lamA, *lamB, *padj, *gpart;
-  double* gacc;
+  float *ckpt, *ustore, *lamA, *lamB, *padj;
+  double *gpart, *gacc;
   size_t bytes;
 };
 
@@ -225,7 +230,7 @@ GradWs carve_grad(const nsgb_plan* plan, int steps, int every, void* ws) {
   g.lamA = cv.take<float>(2 * NN);
   g.lamB = cv.take<float>(2 * NN);
   g.padj = cv.take<float>(NN);
-  g.gpart = cv.take<float>((size_t)every * nblk * 3);
+  g.gpart = cv.take<double>((size_t)every * nblk * 3);
   g.gacc = cv.take<double>(4);
   g.bytes = cv.off;
   return g;
@@ -285,6 +290,7 @@ SolveDev make_solvedev(const nsgb_member& m, void* state) {
   a.theta = m.theta;
   a.theta_len = m.theta_len;
   a.jpart = w.jpart;
+  a.jpart_rows = w.steps;
   a.rhs = w.rhs;
   a.step_ctr = w.ctr;
   a.step_fixed = 0;
@@ -449,6 +455,7 @@ cudaError_t rollout_step(const nsgb_plan* plan, StencilArgs a, const float* us_i
   a.rhs = w.rhs;
   a.u_out = u_out;
   a.jpart = w.jpart;
+  a.jpart_rows = w.steps;
   a.step_ctr = ctr;
   a.step_fixed = step_fixed;
   a.t_from_step = 1;
@@ -660,6 +667,7 @@ int nsgb_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, cons
   a.us_out = w.usA;
   a.rhs = w.rhs;
   a.jpart = w.jpart;
+  a.jpart_rows = w.steps;
   a.theta = theta;
   a.theta_len = theta_len;
   a.step_fixed = 0;
@@ -705,7 +713,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
     std::lock_guard<std::mutex> lk(plan->mu);
     GraphEntry* ge = nullptr;
     for (auto& g : plan->graphs) {
-      if (g.ws == workspace && g.theta == theta && g.theta_len == theta_len && g.chunk == K &&
+      if (g.ws == workspace && g.steps == steps && g.theta == theta && g.theta_len == theta_len && g.chunk == K &&
           g.scheme == a.scheme && std::memcmp(&g.c, &a.c, sizeof(StepConsts)) == 0 &&
           g.tiles[0] == plan->tile_w && g.tiles[1] == plan->tile_h && g.tiles[2] == plan->rows_per_cta &&
           g.tiles[3] == plan->cols_per_cta) {
@@ -738,6 +746,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
       if (ee != cudaSuccess) return cuda_fail(ee, "cudaStreamEndCapture");
       GraphEntry g;
       g.ws = workspace;
+      g.steps = steps;
       g.theta = theta;
       g.theta_len = theta_len;
       g.chunk = K;
@@ -1026,6 +1035,7 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
         b.us_out = w.usB;
         b.rhs = w.rhs;
         b.jpart = w.jpart;
+        b.jpart_rows = w.steps;
         b.step_fixed = 0;
         err = launch_stencil(b, MODE_ROLLOUT, st);
       } else {

@@ -38,6 +38,7 @@ struct StencilArgs {
   float* rhs = nullptr;          // (N,N) div(u*)/dt
   float* u_out = nullptr;        // optional (2,N,N): the projected state u^n
   float* jpart = nullptr;        // per-block partial sums of u_x * f_x, [step][nblk]
+  int jpart_rows = 0;            // rows allocated in jpart (a store beyond is skipped)
   const float* theta = nullptr;  // device theta
   int theta_len = 2;
   const int* step_ctr = nullptr;  // device step base (nullptr: 0); step = base + step_fixed
@@ -102,7 +103,7 @@ struct AdjointArgs {
   const float* u = nullptr;      // (2,N,N) forward state u_s
   float* lam_out = nullptr;      // (2,N,N) lambda_s
   float* rhs = nullptr;          // (N,N) div(lambda_s)/dt
-  float* gpart = nullptr;        // per-block partial theta sensitivities, [step][nblk][3]
+  double* gpart = nullptr;       // per-block partial theta sensitivities, [step][nblk][3]
   const float* theta = nullptr;
   int theta_len = 2;
   int step = 0;                  // forward step index s (forcing time t = s*dt)
@@ -112,7 +113,7 @@ struct AdjointArgs {
   StepConsts c;
 };
 cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
-cudaError_t launch_greduce(const float* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
+cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
 cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st);
 
 }  // namespace nsgb

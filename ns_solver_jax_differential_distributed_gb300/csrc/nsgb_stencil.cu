@@ -166,7 +166,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     if (ty == 0) {
       float v = (tx < nty) ? sRed[tx] : 0.0f;
       v = warp_sum(v);
-      if (tx == 0) {
+      if (tx == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
         const int nblk = gridDim.x * gridDim.y;
         a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
       }

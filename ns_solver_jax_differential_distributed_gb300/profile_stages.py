@@ -1,0 +1,92 @@
+"""Per-stage timing of one solver step (the stage split of the reference's
+solver_profiler.py: advection_diffusion -> the fused stencil, pressure_solve ->
+the three FFT kernels), and the ``ProfileSummary`` / ``benchmark_callable``
+contract of solver_profiler.py:14-61 for host-level timing.
+
+    python -m ns_solver_jax_differential_distributed_gb300.profile_stages --N 4096 --reps 1
+
+runs one warm step and then `reps` launches of each stage kernel with CUDA
+events (cold L2 per launch) and prints the mean time, the achieved bandwidth
+for the stage's algorithmic bytes and the fraction of the measured HBM peak.
+It launches few kernels, so it is the command to capture under ncu.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import time
+from dataclasses import dataclass
+from typing import Callable, List
+
+import numpy as np
+
+
+@dataclass(frozen=True)
+class ProfileSummary:
+    """solver_profiler.py:14-20."""
+    label: str
+    mean_sec: float
+    min_sec: float
+    max_sec: float
+    std_sec: float
+
+
+def benchmark_callable(label: str, fn: Callable, *args, warmup: int = 1, runs: int = 5) -> ProfileSummary:
+    """Warm-up calls, then `runs` timed calls with a device synchronisation
+    after each (solver_profiler.py:36-61)."""
+    import torch
+
+    def block(x):
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+        return x
+
+    for _ in range(max(0, warmup)):
+        block(fn(*args))
+    samples: List[float] = []
+    for _ in range(max(1, runs)):
+        t0 = time.perf_counter()
+        block(fn(*args))
+        samples.append(time.perf_counter() - t0)
+    a = np.array(samples, dtype=np.float64)
+    return ProfileSummary(label, float(a.mean()), float(a.min()), float(a.max()), float(a.std()))
+
+
+def main(argv=None):
+    import torch
+    from . import _build, _native
+    from .workloads import spectral_u0, theta_draw
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--N", type=int, default=4096)
+    ap.add_argument("--scheme", default="central")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--no-flush", action="store_true")
+    ap.add_argument("--tiles", default="", help="tw,th,rows,cols")
+    args = ap.parse_args(argv)
+    _build.build()
+    dev = torch.device("cuda")
+    L = 2 * math.pi
+    u0 = torch.from_numpy(spectral_u0(args.N, min(32, args.N // 4), 0)).to(dev)
+    th = torch.from_numpy(theta_draw(1e-4, 0)).to(dev)
+    if args.tiles:
+        _native.get_plan(args.N, L, dev).set_tiles(*[int(x) for x in args.tiles.split(",")])
+    flush = None if args.no_flush else torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    st = _native.time_stages(u0, th, L, 1e-4, 2.5e-4, args.scheme, args.reps, flush)
+    try:
+        with open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                               "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+    except Exception:
+        peak = 6800.0
+    out = {"N": args.N, "scheme": args.scheme, "tiles": _native.get_plan(args.N, L, dev).tiles(), "stages": {}}
+    for k, ms in st.items():
+        gbs = _native.STAGE_BYTES_PER_CELL[k] * args.N * args.N / (ms * 1e-3) / 1e9
+        out["stages"][k] = {"ms": round(ms, 5), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 3)}
+    out["step_ms"] = round(sum(st.values()), 5)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

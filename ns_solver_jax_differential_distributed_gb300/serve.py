@@ -95,18 +95,25 @@ class _U0Cache:
     def __init__(self, device, K=32, variants=16):
         self.device, self.K, self.variants = device, K, variants
         self._c = {}
+        self._lock = threading.Lock()
 
     def get(self, N: int, seed: int) -> torch.Tensor:
         key = (N, seed % self.variants)
-        if key not in self._c:
-            self._c[key] = torch.from_numpy(spectral_u0(N, min(self.K, N // 4), key[1])).to(self.device)
-        return self._c[key]
+        with self._lock:
+            if key not in self._c:
+                t = torch.from_numpy(spectral_u0(N, min(self.K, N // 4), key[1])).to(self.device)
+                torch.cuda.synchronize(self.device)  # shared by all streams afterwards
+                self._c[key] = t
+            return self._c[key]
 
 
 class Server:
     def __init__(self, device=None, hbm_budget: float = 150e9, slice_steps: int = 32,
                  max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 4):
-        self.device = torch.device(device or "cuda")
+        dev = torch.device(device or "cuda")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        self.device = dev
         self.budget = float(hbm_budget)
         self.slice = int(slice_steps)
         self.max_active_cells = float(max_active_cells)
@@ -139,7 +146,7 @@ class Server:
                 u0 = self.u0.get(r.N, r.seed)
                 th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
                 J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
-                                                      want_u_final=False)
+                                                      want_u_final=False, own_workspace=True)
                 Jh, gh = J.to("cpu", non_blocking=True), g.to("cpu", non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(stream)
