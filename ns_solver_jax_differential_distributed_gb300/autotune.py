@@ -28,7 +28,8 @@ _CACHE_PATH = os.environ.get("NSGB_TUNE_CACHE") or os.path.join(
     os.path.dirname(os.path.abspath(__file__)), "_autotune", "tiles.json")
 _lock = threading.Lock()
 
-STENCIL_TILES = [(32, 8), (64, 8), (64, 16), (128, 8), (32, 16), (64, 32), (128, 16), (32, 32)]
+# the shapes csrc/nsgb_common.cuh instantiates (NSGB_STENCIL_TILES)
+STENCIL_TILES = [(16, 8), (16, 16), (32, 8), (32, 16), (64, 8), (64, 16), (128, 8)]
 ROW_CHOICES = [2, 4, 8, 16]
 COL_CHOICES = [1, 2, 4]
 
@@ -101,7 +102,9 @@ def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, r
                    "cols": results["cols"][cols]},
             "default": list(base)}
     if verbose:
-        print(f"autotune N={N} {scheme}: {best}")
+        print(f"autotune N={N} {scheme}: best {best}")
+        for kind, res in results.items():
+            print(f"  {kind}: " + ", ".join(f"{k}={v * 1e3:.1f}us" for k, v in sorted(res.items(), key=lambda kv: kv[1])))
     with _lock:
         cache = _load()
         cache[key] = best

@@ -25,18 +25,17 @@
 
 namespace nsgb {
 
-template <int SCHEME>
+template <int SCHEME, int TW, int TH>
 __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   extern __shared__ float sm[];
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
   const size_t NN = (size_t)N * N;
-  const int TW = a.tw, TH = a.th;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
-  const int tx = threadIdx.x, ty = threadIdx.y, nty = blockDim.y;
-  const int PW = TW + 6, PH = TH + 6;
-  const int UW = TW + 4, UH = TH + 4;
-  const int SW = TW + 2, SH = TH + 2;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  constexpr int PW = TW + 6, PH = TH + 6;
+  constexpr int UW = TW + 4, UH = TH + 4;
+  constexpr int SW = TW + 2, SH = TH + 2;
   float* sP = sm;
   float* sMx = sP + PH * PW;
   float* sMy = sMx + UH * UW;
@@ -55,6 +54,26 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   const float t = fmul((float)a.step, dt);
   const float A = __ldg(a.theta), B = __ldg(a.theta + 1);
 
+  const bool has_lam = a.lam != nullptr;
+  const bool has_p = a.p != nullptr;
+  if (has_p) {
+    const float* __restrict__ pp = a.p;
+    for2d<PH, PW>(tx, ty, [&](int r, int cc) {
+      sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
+    });
+  }
+  {
+    const float* __restrict__ u = a.u;
+    const float* __restrict__ lam = a.lam;
+    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
+      const int o = r * UW + cc;
+      sUx[o] = __ldg(u + g);
+      sUy[o] = __ldg(u + NN + g);
+      sMx[o] = has_lam ? __ldg(lam + g) : 0.0f;
+      sMy[o] = has_lam ? __ldg(lam + NN + g) : 0.0f;
+    });
+  }
   {
     const int tid = ty * 32 + tx;
     const ForcingRow fr = forcing_time(A, B, t, c);
@@ -73,115 +92,91 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
       sDB[r] = dsig * (-2.0f * cb * sinf(argB) * twopi * t);
     }
   }
-
-  const bool has_lam = a.lam != nullptr;
-  const bool has_p = a.p != nullptr;
-  if (has_p) {
-    for (int r = ty; r < PH; r += nty) {
-      const float* row = a.p + (size_t)((i0 - 3 + r) & M) * N;
-      for (int cc = tx; cc < PW; cc += 32) sP[r * PW + cc] = __ldg(row + ((j0 - 3 + cc) & M));
-    }
-  }
-  for (int r = ty; r < UH; r += nty) {
-    const size_t rowoff = (size_t)((i0 - 2 + r) & M) * N;
-    for (int cc = tx; cc < UW; cc += 32) {
-      const size_t g = rowoff + ((j0 - 2 + cc) & M);
-      const int o = r * UW + cc;
-      sUx[o] = __ldg(a.u + g);
-      sUy[o] = __ldg(a.u + NN + g);
-      sMx[o] = has_lam ? __ldg(a.lam + g) : 0.0f;
-      sMy[o] = has_lam ? __ldg(a.lam + NN + g) : 0.0f;
-    }
-  }
   __syncthreads();
 
   if (has_p) {  // mu = lambda - dt grad p
-    for (int r = ty; r < UH; r += nty) {
-      for (int cc = tx; cc < UW; cc += 32) {
-        const int op = (r + 1) * PW + (cc + 1);
-        const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
-        const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
-        const int o = r * UW + cc;
-        sMx[o] = fsub(sMx[o], fmul(dt, px));
-        sMy[o] = fsub(sMy[o], fmul(dt, py));
-      }
-    }
+    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+      const int op = (r + 1) * PW + (cc + 1);
+      const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
+      const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
+      const int o = r * UW + cc;
+      sMx[o] = fsub(sMx[o], fmul(dt, px));
+      sMy[o] = fsub(sMy[o], fmul(dt, py));
+    });
     __syncthreads();
   }
 
   // theta sensitivities on the interior cells, accumulated in double: the
   // nu term is a small difference of large contributions
   double gA = 0.0, gB = 0.0, gN = 0.0;
-  for (int r = ty; r < TH; r += nty) {
-    for (int cc = tx; cc < TW; cc += 32) {
-      const int o = (r + 2) * UW + (cc + 2);
-      const float w = jscale * sUx[o] + dt * sMx[o];
-      gA += (double)(w * sDA[r]);
-      gB += (double)(w * sDB[r]);
-      const float lux = (sUx[o - UW] + sUx[o + UW] + sUx[o + 1] + sUx[o - 1] - 4.0f * sUx[o]) / c.dx2;
-      const float luy = (sUy[o - UW] + sUy[o + UW] + sUy[o + 1] + sUy[o - 1] - 4.0f * sUy[o]) / c.dx2;
-      gN += (double)dt * ((double)sMx[o] * lux + (double)sMy[o] * luy);
-    }
-  }
+  for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+    const int o = (r + 2) * UW + (cc + 2);
+    const float w = jscale * sUx[o] + dt * sMx[o];
+    gA += (double)(w * sDA[r]);
+    gB += (double)(w * sDB[r]);
+    const float lux = (sUx[o - UW] + sUx[o + UW] + sUx[o + 1] + sUx[o - 1] - 4.0f * sUx[o]) / c.dx2;
+    const float luy = (sUy[o - UW] + sUy[o + UW] + sUy[o + 1] + sUy[o - 1] - 4.0f * sUy[o]) / c.dx2;
+    gN += (double)dt * ((double)sMx[o] * lux + (double)sMy[o] * luy);
+  });
 
   // lambda_s on the tile + 1 halo
   const float inv_h2 = 1.0f / c.h2;
   const float inv_h1 = 1.0f / c.h1;
-  for (int r = ty; r < SH; r += nty) {
-    for (int cc = tx; cc < SW; cc += 32) {
-      const int o = (r + 1) * UW + (cc + 1);
-      const int n = o + UW, s = o - UW, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
-      const float mx = sMx[o], my = sMy[o];
-      const float lmx = (sMx[s] + sMx[n] + sMx[e] + sMx[w] - 4.0f * mx) / c.dx2;
-      const float lmy = (sMy[s] + sMy[n] + sMy[e] + sMy[w] - 4.0f * my) / c.dx2;
-      float atx, aty;
-      if (SCHEME == NSGB_SCHEME_CENTRAL) {
-        const float gxux = (sUx[n] - sUx[s]) * inv_h2, gxuy = (sUy[n] - sUy[s]) * inv_h2;
-        const float gyux = (sUx[e] - sUx[w]) * inv_h2, gyuy = (sUy[e] - sUy[w]) * inv_h2;
-        atx = -(mx * gxux + my * gxuy) + (sMx[n] * sUx[n] - sMx[s] * sUx[s]) * inv_h2 +
-              (sMx[e] * sUy[e] - sMx[w] * sUy[w]) * inv_h2;
-        aty = -(mx * gyux + my * gyuy) + (sMy[n] * sUx[n] - sMy[s] * sUx[s]) * inv_h2 +
-              (sMy[e] * sUy[e] - sMy[w] * sUy[w]) * inv_h2;
-      } else {
-        const float uxo = sUx[o], uyo = sUy[o];
-        const bool mxo = uxo >= 0.f, myo = uyo >= 0.f;
-        // one-sided differences of u at o (the forward's dfx, dfy)
-        const float dxux = (mxo ? uxo - sUx[s] : sUx[n] - uxo) * inv_h1;
-        const float dxuy = (mxo ? uyo - sUy[s] : sUy[n] - uyo) * inv_h1;
-        const float dyux = (myo ? uxo - sUx[w] : sUx[e] - uxo) * inv_h1;
-        const float dyuy = (myo ? uyo - sUy[w] : sUy[e] - uyo) * inv_h1;
-        atx = -(mx * dxux + my * dxuy);
-        aty = -(mx * dyux + my * dyuy);
-        // transposed one-sided operators applied to w = mu_c u_x (x) and mu_c u_y (y)
-        const bool mxn = sUx[n] >= 0.f, mxs = sUx[s] >= 0.f;
-        const bool mye = sUy[e] >= 0.f, myw = sUy[w] >= 0.f;
-#define NSGB_DXT(MU)                                                                    \
-  (((mxo ? MU[o] * uxo : -MU[o] * uxo) - (mxn ? MU[n] * sUx[n] : 0.f) +                \
-    (mxs ? 0.f : MU[s] * sUx[s])) * inv_h1)
-#define NSGB_DYT(MU)                                                                    \
-  (((myo ? MU[o] * uyo : -MU[o] * uyo) - (mye ? MU[e] * sUy[e] : 0.f) +                \
-    (myw ? 0.f : MU[w] * sUy[w])) * inv_h1)
-        atx -= NSGB_DXT(sMx) + NSGB_DYT(sMx);
-        aty -= NSGB_DXT(sMy) + NSGB_DYT(sMy);
-#undef NSGB_DXT
-#undef NSGB_DYT
-      }
-      sLx[r * SW + cc] = mx + dt * (nu * lmx + atx) + jscale * sF[r];
-      sLy[r * SW + cc] = my + dt * (nu * lmy + aty);
+  for2d<SH, SW>(tx, ty, [&](int r, int cc) {
+    const int o = (r + 1) * UW + (cc + 1);
+    const int n = o + UW, s = o - UW, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
+    const float mx = sMx[o], my = sMy[o];
+    const float lmx = (sMx[s] + sMx[n] + sMx[e] + sMx[w] - 4.0f * mx) / c.dx2;
+    const float lmy = (sMy[s] + sMy[n] + sMy[e] + sMy[w] - 4.0f * my) / c.dx2;
+    float atx, aty;
+    if (SCHEME == NSGB_SCHEME_CENTRAL) {
+      const float gxux = (sUx[n] - sUx[s]) * inv_h2, gxuy = (sUy[n] - sUy[s]) * inv_h2;
+      const float gyux = (sUx[e] - sUx[w]) * inv_h2, gyuy = (sUy[e] - sUy[w]) * inv_h2;
+      atx = -(mx * gxux + my * gxuy) + (sMx[n] * sUx[n] - sMx[s] * sUx[s]) * inv_h2 +
+            (sMx[e] * sUy[e] - sMx[w] * sUy[w]) * inv_h2;
+      aty = -(mx * gyux + my * gyuy) + (sMy[n] * sUx[n] - sMy[s] * sUx[s]) * inv_h2 +
+            (sMy[e] * sUy[e] - sMy[w] * sUy[w]) * inv_h2;
+    } else {
+      const float uxo = sUx[o], uyo = sUy[o];
+      const bool mxo = uxo >= 0.f, myo = uyo >= 0.f;
+      // one-sided differences of u at o (the forward's dfx, dfy)
+      const float dxux = (mxo ? uxo - sUx[s] : sUx[n] - uxo) * inv_h1;
+      const float dxuy = (mxo ? uyo - sUy[s] : sUy[n] - uyo) * inv_h1;
+      const float dyux = (myo ? uxo - sUx[w] : sUx[e] - uxo) * inv_h1;
+      const float dyuy = (myo ? uyo - sUy[w] : sUy[e] - uyo) * inv_h1;
+      atx = -(mx * dxux + my * dxuy);
+      aty = -(mx * dyux + my * dyuy);
+      // transposed one-sided operators applied to w = mu_c u_x (x) and mu_c u_y (y)
+      const bool mxn = sUx[n] >= 0.f, mxs = sUx[s] >= 0.f;
+      const bool mye = sUy[e] >= 0.f, myw = sUy[w] >= 0.f;
+      auto dxt = [&](const float* mu) {
+        return ((mxo ? mu[o] * uxo : -mu[o] * uxo) - (mxn ? mu[n] * sUx[n] : 0.f) +
+                (mxs ? 0.f : mu[s] * sUx[s])) * inv_h1;
+      };
+      auto dyt = [&](const float* mu) {
+        return ((myo ? mu[o] * uyo : -mu[o] * uyo) - (mye ? mu[e] * sUy[e] : 0.f) +
+                (myw ? 0.f : mu[w] * sUy[w])) * inv_h1;
+      };
+      atx -= dxt(sMx) + dyt(sMx);
+      aty -= dxt(sMy) + dyt(sMy);
     }
-  }
+    sLx[r * SW + cc] = mx + dt * (nu * lmx + atx) + jscale * sF[r];
+    sLy[r * SW + cc] = my + dt * (nu * lmy + aty);
+  });
   __syncthreads();
 
-  for (int r = ty; r < TH; r += nty) {
-    for (int cc = tx; cc < TW; cc += 32) {
+  {
+    float* __restrict__ lo = a.lam_out;
+    float* __restrict__ rhs = a.rhs;
+    for2d<TH, TW>(tx, ty, [&](int r, int cc) {
       const int o = (r + 1) * SW + (cc + 1);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      a.lam_out[g] = sLx[o];
-      a.lam_out[NN + g] = sLy[o];
+      lo[g] = sLx[o];
+      lo[NN + g] = sLy[o];
       const float gx = fdiv(fsub(sLx[o + SW], sLx[o - SW]), c.h2);
       const float gy = fdiv(fsub(sLy[o + 1], sLy[o - 1]), c.h2);
-      a.rhs[g] = fdiv(fadd(gx, gy), dt);
-    }
+      rhs[g] = fdiv(fadd(gx, gy), dt);
+    });
   }
 
   gA = warp_sum_d(gA);
@@ -194,9 +189,9 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
   __syncthreads();
   if (ty == 0) {
-    double v0 = (tx < nty) ? sRed[tx] : 0.0;
-    double v1 = (tx < nty) ? sRed[8 + tx] : 0.0;
-    double v2 = (tx < nty) ? sRed[16 + tx] : 0.0;
+    double v0 = (tx < 8) ? sRed[tx] : 0.0;
+    double v1 = (tx < 8) ? sRed[8 + tx] : 0.0;
+    double v2 = (tx < 8) ? sRed[16 + tx] : 0.0;
     v0 = warp_sum_d(v0);
     v1 = warp_sum_d(v1);
     v2 = warp_sum_d(v2);
@@ -217,21 +212,30 @@ static size_t adjoint_smem(int tw, int th) {
   return f * sizeof(float) + 24 * sizeof(double) + 8;
 }
 
-template <int SCHEME>
+template <int SCHEME, int TW, int TH>
 static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(k_adjoint<SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_adjoint<SCHEME, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     configured = true;
   }
-  const dim3 grid(a.c.N / a.tw, a.c.N / a.th);
-  k_adjoint<SCHEME><<<grid, dim3(32, 8), adjoint_smem(a.tw, a.th), st>>>(a);
+  const dim3 grid(a.c.N / TW, a.c.N / TH);
+  k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), adjoint_smem(TW, TH), st>>>(a);
   return cudaGetLastError();
 }
 
+template <int SCHEME>
+static cudaError_t launch_adjoint_s(const AdjointArgs& a, cudaStream_t st) {
+#define NSGB_TILE_CASE(W, H) \
+  if (a.tw == W && a.th == H) return launch_adjoint_t<SCHEME, W, H>(a, st);
+  NSGB_STENCIL_TILES(NSGB_TILE_CASE)
+#undef NSGB_TILE_CASE
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
-  return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_t<NSGB_SCHEME_CENTRAL>(a, st)
-                                         : launch_adjoint_t<NSGB_SCHEME_UPWIND>(a, st);
+  return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_s<NSGB_SCHEME_CENTRAL>(a, st)
+                                         : launch_adjoint_s<NSGB_SCHEME_UPWIND>(a, st);
 }
 
 // Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double).

@@ -49,6 +49,8 @@ int ilog2(int n) {
   return l;
 }
 size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+// Transposed half spectrum: N/2 + 1 rows of N complex values.
+size_t spec_floats(int N) { return (size_t)(N / 2 + 1) * N * 2; }
 
 struct GraphEntry {
   const void* ws = nullptr;
@@ -99,10 +101,8 @@ void default_tiles(int N, int out[4]) {
 
 int check_tiles(int N, int tw, int th, int rows, int cols) {
   const int T = N / (N < 16 ? N : 16);
-  if (!is_pow2(tw) || tw < 16 || tw > 128 || tw > N)
-    return fail(NSGB_ERR_INVALID_ARG, "stencil tile width %d must be a power of two in [16, min(128, N)]", tw);
-  if (!is_pow2(th) || th < 2 || th > 32 || th > N)
-    return fail(NSGB_ERR_INVALID_ARG, "stencil tile height %d must be a power of two in [2, min(32, N)]", th);
+  if (!stencil_tile_supported(tw, th) || tw > N || th > N)
+    return fail(NSGB_ERR_INVALID_ARG, "stencil tile %dx%d is not an instantiated shape for N=%d", tw, th, N);
   if (!is_pow2(rows) || rows < 2 || rows > N || (rows / 2) * T > 1024 ||
       fft_rows_smem_bytes(N, rows) > 200 * 1024)
     return fail(NSGB_ERR_INVALID_ARG, "rows_per_cta %d invalid for N=%d", rows, N);
@@ -202,7 +202,7 @@ RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
   w.usB = cv.take<float>(2 * NN);
   w.p = cv.take<float>(NN);
   w.rhs = cv.take<float>(NN);
-  w.spec = cv.take<float>(NN);
+  w.spec = cv.take<float>(spec_floats(plan->N));
   w.jpart = cv.take<float>((size_t)(steps > 0 ? steps : 1) * nblk);
   w.jsteps = cv.take<double>(steps > 0 ? steps : 1);
   w.steps = steps > 0 ? steps : 1;
@@ -563,7 +563,7 @@ int nsgb_plan_get_tiles(const nsgb_plan* plan, int out[4]) {
 }
 
 size_t nsgb_poisson_workspace_bytes(const nsgb_plan* plan) {
-  return plan ? align_up((size_t)plan->N * plan->N * sizeof(float)) : 0;
+  return plan ? align_up(spec_floats(plan->N) * sizeof(float)) : 0;
 }
 
 size_t nsgb_step_workspace_bytes(const nsgb_plan* plan) {

@@ -83,6 +83,23 @@ __device__ __forceinline__ void forcing_fx_grad(int i, const ForcingRow& f, cons
   dsig = fx * d * d / (s2 * f.sig);
 }
 
+// Visit the cells (r, cc) of an H x W tile with a 32 x 8 thread block; the
+// trip counts are compile-time, so the loop unrolls completely.
+template <int H, int W, class F>
+__device__ __forceinline__ void for2d(int tx, int ty, F&& f) {
+#pragma unroll
+  for (int r0 = 0; r0 < H; r0 += 8) {
+#pragma unroll
+    for (int c0 = 0; c0 < W; c0 += 32) {
+      const int r = r0 + ty, cc = c0 + tx;
+      if ((H % 8 == 0 || r < H) && (W % 32 == 0 || cc < W)) f(r, cc);
+    }
+  }
+}
+
+// Stencil tile shapes (width x height) the kernels are instantiated for.
+#define NSGB_STENCIL_TILES(X) X(16, 8) X(16, 16) X(32, 8) X(32, 16) X(64, 8) X(64, 16) X(128, 8)
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -4,15 +4,16 @@
 // The real N x N right-hand side is transformed in two passes:
 //   rows (along y, contiguous): two real rows a, b are packed as a + i b, one
 //     complex length-N FFT gives both half spectra X_a[k], X_b[k], k=0..N/2.
-//     The half spectrum is stored transposed, spec[k][i] (k = 0..N/2-1,
-//     i contiguous), with the real DC and Nyquist values of row i packed as
-//     spec[0][i] = (X_i[0], X_i[N/2]).  spec holds N*N/2 complex = N*N floats,
-//     the size of the real field.
+//     The half spectrum is stored transposed, spec[k][i] (k = 0..N/2, i
+//     contiguous): N/2 + 1 rows of N complex values.
 //   columns (along x): each spec[k] row is transformed, multiplied by
 //     -1/|k|^2 (0 at k = 0; NS_solver.py:521, 525-526), transformed back and
-//     written in place.  The packed row k = 0 carries two real-valued columns,
-//     which are separated with Hermitian symmetry, scaled by their own
-//     multipliers and recombined.
+//     written in place.  Every ky column has its own row -- in particular the
+//     DC and Nyquist columns are never packed together -- so a field that is
+//     constant along y keeps exactly zero spectrum at ky != 0, as the
+//     reference's C2C transforms do (its zero-state runs stay exactly
+//     y-independent, which the upwind study at the diffusive stability limit
+//     relies on).
 //   rows again: the inverse two-for-one C2R transform writes p.
 // All scale factors (the 1/2 of the two-for-one split and the 1/N^2 of ifft2)
 // are powers of two folded into the spectral multiplier, so they round
@@ -66,21 +67,16 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
 
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
-  for (int e = tid; e < RB * H; e += nth) {
+  for (int e = tid; e < RB * (H + 1); e += nth) {
     const int r = e & (RB - 1);
     const int k = e / RB;
     const float* pre = smem + (r >> 1) * pair_stride<N>();
     const float* pim = pre + PL;
-    float2 out;
-    if (k == 0) {
-      out = (r & 1) ? make_float2(2.0f * pim[pad(0)], 2.0f * pim[pad(H)])
-                    : make_float2(2.0f * pre[pad(0)], 2.0f * pre[pad(H)]);
-    } else {
-      const float zr = pre[pad(k)], zi = pim[pad(k)];
-      const float wr = pre[pad(N - k)], wi = pim[pad(N - k)];
-      out = (r & 1) ? make_float2(zi + wi, wr - zr)   // 2 X_b[k]
-                    : make_float2(zr + wr, zi - wi);  // 2 X_a[k]
-    }
+    const int kn = (N - k) & (N - 1);
+    const float zr = pre[pad(k)], zi = pim[pad(k)];
+    const float wr = pre[pad(kn)], wi = pim[pad(kn)];
+    // 2 X_a[k] = Z[k] + conj(Z[N-k]);  2 X_b[k] = -i (Z[k] - conj(Z[N-k]))
+    const float2 out = (r & 1) ? make_float2(zi + wi, wr - zr) : make_float2(zr + wr, zi - wi);
     spec[(size_t)k * N + i0 + r] = out;
   }
 }
@@ -105,7 +101,10 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
   const int j = threadIdx.x, y = threadIdx.y;
   float* sre = smem + y * pair_stride<N>();
   float* sim = sre + PL;
-  const int ky = blockIdx.x * blockDim.y + y;
+  // N/2 + 1 rows; the last CTA may hold rows past N/2, which recompute row
+  // N/2 and do not store.
+  const int kreq = blockIdx.x * blockDim.y + y;
+  const int ky = kreq < H ? kreq : H;
   float2* row = spec + (size_t)ky * N;
 
   float2 a[E];
@@ -114,49 +113,17 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
   fft::block_fft<N, false>(a, sre, sim, j, tw);
 
   const float k2y = __ldg(k2 + ky);
-  if (blockIdx.x == 0) {
-    // The CTA holding ky = 0: its packed row needs C[-m] from other threads.
-    __syncthreads();
 #pragma unroll
-    for (int s = 0; s < E; ++s) {
-      const int idx = pad(j + s * T);
-      sre[idx] = a[s].x;
-      sim[idx] = a[s].y;
-    }
-    __syncthreads();
-    if (ky == 0) {
-      const float k2n = __ldg(k2 + H);
-#pragma unroll
-      for (int s = 0; s < E; ++s) {
-        const int m = j + s * T;
-        const int mm = pad((N - m) & (N - 1));
-        const float2 cm = make_float2(sre[mm], -sim[mm]);  // conj(C[-m])
-        const float k2x = __ldg(k2 + m);
-        const float g0 = poisson_mult(k2x, 0.0f, scale);
-        const float gn = poisson_mult(k2x, k2n, scale);
-        // C' = ((C + conj(C[-m])) g0 + (C - conj(C[-m])) gn) / 2
-        const float2 sp = cadd(a[s], cm), sm = csub(a[s], cm);
-        a[s] = make_float2(0.5f * (sp.x * g0 + sm.x * gn), 0.5f * (sp.y * g0 + sm.y * gn));
-      }
-    } else {
-#pragma unroll
-      for (int s = 0; s < E; ++s) {
-        const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
-        a[s] = make_float2(a[s].x * g, a[s].y * g);
-      }
-    }
-    __syncthreads();
-  } else {
-#pragma unroll
-    for (int s = 0; s < E; ++s) {
-      const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
-      a[s] = make_float2(a[s].x * g, a[s].y * g);
-    }
+  for (int s = 0; s < E; ++s) {
+    const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
+    a[s] = make_float2(a[s].x * g, a[s].y * g);
   }
-
   fft::block_fft<N, true>(a, sre, sim, j, tw);
+  __syncthreads();  // rows clamped to N/2 were loaded by other threads
+  if (kreq <= H) {
 #pragma unroll
-  for (int s = 0; s < E; ++s) row[j + s * T] = a[s];
+    for (int s = 0; s < E; ++s) row[j + s * T] = a[s];
+  }
 }
 
 // ---------------------------------------------------------------- rows inv --
@@ -174,14 +141,14 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
 
-  // Stage the RB half-spectrum rows: pair buffer (r>>1) holds X_a at [0,H)
-  // and X_b at [H, N).
-  for (int e = tid; e < RB * H; e += nth) {
+  // Stage the RB half-spectrum rows: pair buffer (r>>1) holds X_a[k] at k
+  // and X_b[k] at H + 1 + k, k = 0..H.
+  for (int e = tid; e < RB * (H + 1); e += nth) {
     const int r = e & (RB - 1);
     const int k = e / RB;
     const float2 v = __ldg(spec + (size_t)k * N + i0 + r);
     float* pre = smem + (r >> 1) * pair_stride<N>();
-    const int idx = pad((r & 1) * H + k);
+    const int idx = pad((r & 1) * (H + 1) + k);
     pre[idx] = v.x;
     pre[PL + idx] = v.y;
   }
@@ -194,17 +161,17 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   for (int s = 0; s < E; ++s) {
     const int m = j + s * T;
     float2 z;
-    if (m == 0) {
-      z = make_float2(sre[pad(0)], sre[pad(H)]);
-    } else if (m == H) {
-      z = make_float2(sim[pad(0)], sim[pad(H)]);
+    if (m == 0 || m == H) {
+      // DC and Nyquist of a real row are real: their imaginary parts (rounding
+      // noise of the column pass) are dropped, as Re(ifft2) drops them.
+      z = make_float2(sre[pad(m)], sre[pad(H + 1 + m)]);
     } else if (m < H) {
       const float2 xa = make_float2(sre[pad(m)], sim[pad(m)]);
-      const float2 xb = make_float2(sre[pad(H + m)], sim[pad(H + m)]);
+      const float2 xb = make_float2(sre[pad(H + 1 + m)], sim[pad(H + 1 + m)]);
       z = make_float2(xa.x - xb.y, xa.y + xb.x);  // X_a + i X_b
     } else {
       const float2 xa = make_float2(sre[pad(N - m)], sim[pad(N - m)]);
-      const float2 xb = make_float2(sre[pad(H + N - m)], sim[pad(H + N - m)]);
+      const float2 xb = make_float2(sre[pad(H + 1 + N - m)], sim[pad(H + 1 + N - m)]);
       z = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj(X_a) + i conj(X_b)
     }
     a[s] = z;
@@ -275,7 +242,7 @@ static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, in
     configured = true;
   }
   if (sv) {
-    const dim3 gr(N / (2 * P), count), gc((N / 2) / KB, count);
+    const dim3 gr(N / (2 * P), count), gc((N / 2) / KB + 1, count);
     k_rows_fwd_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
     k_cols_b<N><<<gc, dim3(T, KB), smem_cols, st>>>(sv, L.tw, L.k2, L.scale);
     k_rows_inv_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
@@ -285,7 +252,7 @@ static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, in
     k_rows_fwd<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.rhs, L.spec, L.tw);
   }
   if (L.do_cols) {
-    k_cols<N><<<(N / 2) / KB, dim3(T, KB), smem_cols, st>>>(L.spec, L.tw, L.k2, L.scale);
+    k_cols<N><<<(N / 2) / KB + 1, dim3(T, KB), smem_cols, st>>>(L.spec, L.tw, L.k2, L.scale);
   }
   if (L.p) {
     k_rows_inv<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.spec, L.p, L.tw);

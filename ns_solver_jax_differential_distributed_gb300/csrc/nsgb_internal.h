@@ -11,7 +11,7 @@ namespace nsgb {
 // ------------------------------------------------------------------ FFT --
 struct FftLaunch {
   const float* rhs = nullptr;  // rows forward input (nullptr: skip the pass)
-  float2* spec = nullptr;      // transposed half spectrum, (N/2) x N complex
+  float2* spec = nullptr;      // transposed half spectrum, (N/2 + 1) x N complex
   bool do_cols = true;         // column transform + Poisson multiplier
   float* p = nullptr;          // rows inverse output (nullptr: skip the pass)
   const float2* tw = nullptr;  // twiddles W_N[m], m = 0..N-1
@@ -51,6 +51,7 @@ struct StencilArgs {
 };
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st);
 int stencil_nblocks(int N, int tw, int th);
+bool stencil_tile_supported(int tw, int th);
 
 // ------------------------------------------------------------- ensembles --
 // Device-resident description of one member of an ensemble advanced by

@@ -42,18 +42,17 @@ __device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, fl
   }
 }
 
-template <int SCHEME, int MODE>
+template <int SCHEME, int MODE, int TW, int TH>
 __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off = 0) {
   extern __shared__ float sm[];
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
   const size_t NN = (size_t)N * N;
-  const int TW = a.tw, TH = a.th;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
-  const int tx = threadIdx.x, ty = threadIdx.y, nty = blockDim.y;
-  const int PW = TW + 6, PH = TH + 6;
-  const int UW = TW + 4, UH = TH + 4;
-  const int SW = TW + 2, SH = TH + 2;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  constexpr int PW = TW + 6, PH = TH + 6;
+  constexpr int UW = TW + 4, UH = TH + 4;
+  constexpr int SW = TW + 2, SH = TH + 2;
   float* sP = sm;
   float* sUx = sP + PH * PW;
   float* sUy = sUx + UH * UW;
@@ -70,6 +69,23 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   }
   const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
 
+  // Tile loads: compile-time trip counts, so every load of a thread is in
+  // flight before the first shared-memory store.
+  const bool has_p = a.p != nullptr;
+  if (has_p) {
+    const float* __restrict__ pp = a.p;
+    for2d<PH, PW>(tx, ty, [&](int r, int cc) {
+      sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
+    });
+  }
+  {
+    const float* __restrict__ us = a.us;
+    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
+      sUx[r * UW + cc] = __ldg(us + g);
+      sUy[r * UW + cc] = __ldg(us + NN + g);
+    });
+  }
   if (MODE == MODE_ROLLOUT) {
     const int tid = ty * 32 + tx;
     if (tid < SH) {
@@ -77,86 +93,67 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
       sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
     }
   }
-  const bool has_p = a.p != nullptr;
-  if (has_p) {
-    for (int r = ty; r < PH; r += nty) {
-      const float* row = a.p + (size_t)((i0 - 3 + r) & M) * N;
-      for (int cc = tx; cc < PW; cc += 32) sP[r * PW + cc] = __ldg(row + ((j0 - 3 + cc) & M));
-    }
-  }
-  for (int r = ty; r < UH; r += nty) {
-    const size_t rowoff = (size_t)((i0 - 2 + r) & M) * N;
-    for (int cc = tx; cc < UW; cc += 32) {
-      const size_t g = rowoff + ((j0 - 2 + cc) & M);
-      sUx[r * UW + cc] = __ldg(a.us + g);
-      sUy[r * UW + cc] = __ldg(a.us + NN + g);
-    }
-  }
   __syncthreads();
 
   // 1. pending projection u^n = u* - dt * grad p
   if (has_p) {
-    for (int r = ty; r < UH; r += nty) {
-      for (int cc = tx; cc < UW; cc += 32) {
-        const int op = (r + 1) * PW + (cc + 1);
-        const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
-        const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
-        const int ou = r * UW + cc;
-        sUx[ou] = fsub(sUx[ou], fmul(c.dt, px));
-        sUy[ou] = fsub(sUy[ou], fmul(c.dt, py));
-      }
-    }
+    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+      const int op = (r + 1) * PW + (cc + 1);
+      const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
+      const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
+      const int ou = r * UW + cc;
+      sUx[ou] = fsub(sUx[ou], fmul(c.dt, px));
+      sUy[ou] = fsub(sUy[ou], fmul(c.dt, py));
+    });
     __syncthreads();
   }
 
   // 2. objective partial on the state before the step; optional state output
   float jacc = 0.0f;
-  for (int r = ty; r < TH; r += nty) {
-    for (int cc = tx; cc < TW; cc += 32) {
-      const int ou = (r + 2) * UW + (cc + 2);
-      if (MODE == MODE_ROLLOUT) jacc += sUx[ou] * sF[r + 1];
-      if (a.u_out) {
-        const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-        a.u_out[g] = sUx[ou];
-        a.u_out[NN + g] = sUy[ou];
-      }
+  for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+    const int ou = (r + 2) * UW + (cc + 2);
+    if (MODE == MODE_ROLLOUT) jacc += sUx[ou] * sF[r + 1];
+    if (a.u_out) {
+      const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
+      a.u_out[g] = sUx[ou];
+      a.u_out[NN + g] = sUy[ou];
     }
-  }
+  });
 
   // 3. u*^{n+1} on the tile + 1 halo
-  for (int r = ty; r < SH; r += nty) {
-    for (int cc = tx; cc < SW; cc += 32) {
-      const int o = (r + 1) * UW + (cc + 1);
-      const float ux = sUx[o], uy = sUy[o];
-      const float lapx = lap5(sUx, o, UW, c), lapy = lap5(sUy, o, UW, c);
-      const float advx = adv5<SCHEME>(sUx, o, UW, ux, uy, c);
-      const float advy = adv5<SCHEME>(sUy, o, UW, ux, uy, c);
-      float fx, fy;
-      if (MODE == MODE_ROLLOUT) {
-        fx = sF[r];
-        fy = 0.0f;
-      } else {
-        const size_t g = (size_t)((i0 - 1 + r) & M) * N + ((j0 - 1 + cc) & M);
-        fx = __ldg(a.f + g);
-        fy = __ldg(a.f + NN + g);
-      }
-      sSx[r * SW + cc] = fadd(ux, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
-      sSy[r * SW + cc] = fadd(uy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+  for2d<SH, SW>(tx, ty, [&](int r, int cc) {
+    const int o = (r + 1) * UW + (cc + 1);
+    const float ux = sUx[o], uy = sUy[o];
+    const float lapx = lap5(sUx, o, UW, c), lapy = lap5(sUy, o, UW, c);
+    const float advx = adv5<SCHEME>(sUx, o, UW, ux, uy, c);
+    const float advy = adv5<SCHEME>(sUy, o, UW, ux, uy, c);
+    float fx, fy;
+    if (MODE == MODE_ROLLOUT) {
+      fx = sF[r];
+      fy = 0.0f;
+    } else {
+      const size_t g = (size_t)((i0 - 1 + r) & M) * N + ((j0 - 1 + cc) & M);
+      fx = __ldg(a.f + g);
+      fy = __ldg(a.f + NN + g);
     }
-  }
+    sSx[r * SW + cc] = fadd(ux, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
+    sSy[r * SW + cc] = fadd(uy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+  });
   __syncthreads();
 
   // 4. write u*^{n+1} and div(u*^{n+1}) / dt
-  for (int r = ty; r < TH; r += nty) {
-    for (int cc = tx; cc < TW; cc += 32) {
+  {
+    float* __restrict__ uso = a.us_out;
+    float* __restrict__ rhs = a.rhs;
+    for2d<TH, TW>(tx, ty, [&](int r, int cc) {
       const int o = (r + 1) * SW + (cc + 1);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      a.us_out[g] = sSx[o];
-      a.us_out[NN + g] = sSy[o];
+      uso[g] = sSx[o];
+      uso[NN + g] = sSy[o];
       const float gx = fdiv(fsub(sSx[o + SW], sSx[o - SW]), c.h2);
       const float gy = fdiv(fsub(sSy[o + 1], sSy[o - 1]), c.h2);
-      a.rhs[g] = fdiv(fadd(gx, gy), c.dt);
-    }
+      rhs[g] = fdiv(fadd(gx, gy), c.dt);
+    });
   }
 
   if (MODE == MODE_ROLLOUT) {
@@ -164,7 +161,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     if (tx == 0) sRed[ty] = jacc;
     __syncthreads();
     if (ty == 0) {
-      float v = (tx < nty) ? sRed[tx] : 0.0f;
+      float v = (tx < 8) ? sRed[tx] : 0.0f;
       v = warp_sum(v);
       if (tx == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
         const int nblk = gridDim.x * gridDim.y;
@@ -174,19 +171,26 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   }
 }
 
-template <int SCHEME, int MODE>
+template <int SCHEME, int MODE, int TW, int TH>
 __global__ void __launch_bounds__(256) k_stencil(const StencilArgs a) {
-  stencil_body<SCHEME, MODE>(a);
+  stencil_body<SCHEME, MODE, TW, TH>(a);
 }
 
 // Ensemble variant: blockIdx.z selects the solve, `variant` its argument set.
-template <int SCHEME>
+template <int SCHEME, int TW, int TH>
 __global__ void __launch_bounds__(256) k_stencil_batch(const SolveDev* __restrict__ solves, int variant,
                                                       int step_off) {
-  stencil_body<SCHEME, MODE_ROLLOUT>(solves[blockIdx.z].st[variant], step_off);
+  stencil_body<SCHEME, MODE_ROLLOUT, TW, TH>(solves[blockIdx.z].st[variant], step_off);
 }
 
 int stencil_nblocks(int N, int tw, int th) { return (N / tw) * (N / th); }
+
+bool stencil_tile_supported(int tw, int th) {
+#define NSGB_TILE_OK(W, H) if (tw == W && th == H) return true;
+  NSGB_STENCIL_TILES(NSGB_TILE_OK)
+#undef NSGB_TILE_OK
+  return false;
+}
 
 static size_t stencil_smem(int tw, int th) {
   const size_t f = (size_t)(th + 6) * (tw + 6) + 2 * (size_t)(th + 4) * (tw + 4) +
@@ -194,46 +198,66 @@ static size_t stencil_smem(int tw, int th) {
   return f * sizeof(float);
 }
 
-template <int SCHEME, int MODE>
+template <int SCHEME, int MODE, int TW, int TH>
 static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(k_stencil<SCHEME, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_stencil<SCHEME, MODE, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          160 * 1024);
     configured = true;
   }
-  const dim3 grid(a.c.N / a.tw, a.c.N / a.th);
-  k_stencil<SCHEME, MODE><<<grid, dim3(32, 8), stencil_smem(a.tw, a.th), st>>>(a);
+  const dim3 grid(a.c.N / TW, a.c.N / TH);
+  k_stencil<SCHEME, MODE, TW, TH><<<grid, dim3(32, 8), stencil_smem(TW, TH), st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int SCHEME, int TW, int TH>
+static cudaError_t launch_stencil_batch_t(const SolveDev* solves, int count, int variant, int step_off, int N,
+                                          cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaFuncSetAttribute(k_stencil_batch<SCHEME, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         160 * 1024);
+    configured = true;
+  }
+  const dim3 grid(N / TW, N / TH, count);
+  k_stencil_batch<SCHEME, TW, TH><<<grid, dim3(32, 8), stencil_smem(TW, TH), st>>>(solves, variant, step_off);
   return cudaGetLastError();
 }
 
 template <int SCHEME>
-static cudaError_t launch_stencil_batch_t(const SolveDev* solves, int count, int variant, int step_off, int N,
+static cudaError_t launch_stencil_batch_s(const SolveDev* solves, int count, int variant, int step_off, int N,
                                           int tw, int th, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_stencil_batch<SCHEME>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    configured = true;
-  }
-  const dim3 grid(N / tw, N / th, count);
-  k_stencil_batch<SCHEME><<<grid, dim3(32, 8), stencil_smem(tw, th), st>>>(solves, variant, step_off);
-  return cudaGetLastError();
+#define NSGB_TILE_CASE(W, H) \
+  if (tw == W && th == H) return launch_stencil_batch_t<SCHEME, W, H>(solves, count, variant, step_off, N, st);
+  NSGB_STENCIL_TILES(NSGB_TILE_CASE)
+#undef NSGB_TILE_CASE
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_stencil_batch(const SolveDev* solves, int count, int variant, int step_off, int scheme, int N,
                                  int tw, int th, cudaStream_t st) {
   return scheme == NSGB_SCHEME_CENTRAL
-             ? launch_stencil_batch_t<NSGB_SCHEME_CENTRAL>(solves, count, variant, step_off, N, tw, th, st)
-             : launch_stencil_batch_t<NSGB_SCHEME_UPWIND>(solves, count, variant, step_off, N, tw, th, st);
+             ? launch_stencil_batch_s<NSGB_SCHEME_CENTRAL>(solves, count, variant, step_off, N, tw, th, st)
+             : launch_stencil_batch_s<NSGB_SCHEME_UPWIND>(solves, count, variant, step_off, N, tw, th, st);
+}
+
+template <int SCHEME, int MODE>
+static cudaError_t launch_stencil_s(const StencilArgs& a, cudaStream_t st) {
+#define NSGB_TILE_CASE(W, H) \
+  if (a.tw == W && a.th == H) return launch_stencil_t<SCHEME, MODE, W, H>(a, st);
+  NSGB_STENCIL_TILES(NSGB_TILE_CASE)
+#undef NSGB_TILE_CASE
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st) {
   if (a.scheme == NSGB_SCHEME_CENTRAL) {
-    return mode == MODE_ROLLOUT ? launch_stencil_t<NSGB_SCHEME_CENTRAL, MODE_ROLLOUT>(a, st)
-                                : launch_stencil_t<NSGB_SCHEME_CENTRAL, MODE_FIELD>(a, st);
+    return mode == MODE_ROLLOUT ? launch_stencil_s<NSGB_SCHEME_CENTRAL, MODE_ROLLOUT>(a, st)
+                                : launch_stencil_s<NSGB_SCHEME_CENTRAL, MODE_FIELD>(a, st);
   }
-  return mode == MODE_ROLLOUT ? launch_stencil_t<NSGB_SCHEME_UPWIND, MODE_ROLLOUT>(a, st)
-                              : launch_stencil_t<NSGB_SCHEME_UPWIND, MODE_FIELD>(a, st);
+  return mode == MODE_ROLLOUT ? launch_stencil_s<NSGB_SCHEME_UPWIND, MODE_ROLLOUT>(a, st)
+                              : launch_stencil_s<NSGB_SCHEME_UPWIND, MODE_FIELD>(a, st);
 }
 
 // ------------------------------------------------------------ projection --
