@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "nsgb_fft.cuh"
 #include "nsgb_internal.h"
 
 using namespace nsgb;
@@ -126,6 +127,22 @@ int check_phys(const nsgb_phys* ph) {
   return NSGB_OK;
 }
 
+// Correctly rounded float reciprocal of d: the float nearest 1/d, chosen among
+// the neighbours of float(1/d) by the exact (double) residual |r*d - 1|.
+float recip_rn(float d) {
+  float r = (float)(1.0 / (double)d);
+  float best = r;
+  double err = std::fabs((double)r * (double)d - 1.0);
+  for (float c : {std::nextafter(r, -INFINITY), std::nextafter(r, INFINITY)}) {
+    const double e = std::fabs((double)c * (double)d - 1.0);
+    if (e < err) {
+      err = e;
+      best = c;
+    }
+  }
+  return best;
+}
+
 // Constants as float32, the way the reference's Python scalars enter its
 // float32 expressions (dx, 2*dx and dx**2 are computed in double first).
 StepConsts make_consts(const nsgb_plan* plan, const nsgb_phys* ph) {
@@ -143,6 +160,10 @@ StepConsts make_consts(const nsgb_plan* plan, const nsgb_phys* ph) {
   c.sigma0 = ph ? (float)ph->sigma0 : 0.1f;
   c.C = ph ? (float)ph->C : 1.0f;
   c.jscale = ph ? (float)(ph->dt * dx * dx) : 0.0f;
+  c.rh1 = recip_rn(c.h1);
+  c.rh2 = recip_rn(c.h2);
+  c.rdx2 = recip_rn(c.dx2);
+  c.rdt = recip_rn(c.dt);
   return c;
 }
 
@@ -491,10 +512,18 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   p->rows_per_cta = t[2];
   p->cols_per_cta = t[3];
 
-  std::vector<float2> tw(N);
-  for (int m = 0; m < N; ++m) {
-    const double ang = -2.0 * M_PI * (double)m / (double)N;
-    tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+  // Per-pass twiddle tables of the Stockham FFT (layout in nsgb_fft.cuh):
+  // the pass with stride ns and radix rp stores W_{ns*rp}^{bm*r} at
+  // off + r*ns + bm, computed in double and rounded to float.
+  const int ntw = nsgb::fft::tw_entries(N);
+  std::vector<float2> tw(ntw, make_float2(1.f, 0.f));
+  for (int ns = 16, off = 0; ns < N; off += (N / ns >= 16 ? 16 : N / ns) * ns, ns *= 16) {
+    const int rp = N / ns >= 16 ? 16 : N / ns;
+    for (int r = 1; r < rp; ++r)
+      for (int bm = 0; bm < ns; ++bm) {
+        const double ang = -2.0 * M_PI * (double)bm * r / ((double)ns * rp);
+        tw[off + r * ns + bm] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+      }
   }
   // k = 2 pi fftfreq(N, dx) in float32 as NS_solver.py:518-519 evaluates it:
   // (m / float32(dx*N)) * 2 * float32(pi), then squared in float32.
@@ -509,9 +538,9 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
     volatile float kk = k * k;
     k2[m] = kk;
   }
-  cudaError_t e = cudaMalloc(&p->tw, N * sizeof(float2));
+  cudaError_t e = cudaMalloc(&p->tw, ntw * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&p->k2, N * sizeof(float));
-  if (e == cudaSuccess) e = cudaMemcpy(p->tw, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->tw, tw.data(), ntw * sizeof(float2), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->k2, k2.data(), N * sizeof(float), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(p->tw);

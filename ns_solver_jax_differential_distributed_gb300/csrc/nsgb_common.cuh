@@ -18,6 +18,19 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 
+// x / d rounded to nearest, for a divisor d whose correctly rounded
+// reciprocal rd = RN(1/d) is precomputed: q = RN(x*rd) is within one ulp of
+// x/d, the remainder x - q*d is exact in one FMA, and RN(q + r*rd) = RN(x/d)
+// (Markstein's theorem, binary floating point, normal range).  Three
+// instructions instead of a full IEEE division; the stencil tests compare the
+// results bit for bit with NumPy's divisions.  (A -0 numerator gives +0, an
+// infinite one NaN.)
+__device__ __forceinline__ float divc(float x, float d, float rd) {
+  const float q = __fmul_rn(x, rd);
+  const float r = __fmaf_rn(-q, d, x);
+  return __fmaf_rn(r, rd, q);
+}
+
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -40,6 +53,8 @@ struct StepConsts {
   float nu;     // float32(nu) (used when theta has 2 entries)
   float mu0, sigma0, C;
   float jscale; // dt * dx**2 in double, applied at the reduction
+  // correctly rounded reciprocals of the divisors (for divc)
+  float rh1, rh2, rdx2, rdt;
 };
 
 // Gaussian forcing fx at row i for time t (NS_solver.py:621-627):

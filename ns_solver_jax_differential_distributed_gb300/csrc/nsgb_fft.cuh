@@ -10,8 +10,10 @@
 // radix 2/4/8 when log2(N) is not a multiple of 4).  Between passes the values
 // are exchanged through shared memory, split into real and imaginary planes
 // and padded by one word every 16 (index i -> i + i/16), which makes the pass
-// writes bank-conflict free.  Twiddles come from a table W_N[m] =
-// exp(-2 pi i m / N) computed on the host in double precision.
+// writes bank-conflict free.  Twiddles come from per-pass tables computed on
+// the host in double precision and rounded to float: the pass with stride NS
+// and radix RP stores W_{NS*RP}^{bm*r} at [r*NS + bm], so the twiddle loads of
+// a warp (consecutive bm) are contiguous.
 #pragma once
 
 #include "nsgb_common.cuh"
@@ -93,6 +95,20 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
   for (int k = 0; k < R; ++k) a[k] = b[k];
 }
 
+// Offset (in complex entries) of the twiddle table of the pass with stride
+// NS: the passes before it all have radix 16 and stride 16, 256, ...
+__host__ __device__ constexpr int tw_offset(int NS) {
+  int off = 0;
+  for (int ns = 16; ns < NS; ns *= 16) off += 16 * ns;
+  return off;
+}
+// Total twiddle entries for length N.
+__host__ __device__ constexpr int tw_entries(int N) {
+  int off = 0;
+  for (int ns = 16; ns < N; ns *= 16) off += ((N / ns >= 16) ? 16 : N / ns) * ns;
+  return off > 0 ? off : 1;
+}
+
 // One Stockham pass (stride NS) and, recursively, the remaining passes.
 template <int N, int NS, bool INV>
 __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sre,
@@ -104,7 +120,6 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sr
   constexpr int RP = REM >= 16 ? 16 : REM;
   constexpr int Q = E / RP;
   constexpr bool LAST = (NS * RP == N);
-  constexpr int TWS = N / (NS * RP);
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     const int b = j + q * T;
@@ -113,9 +128,10 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sr
     for (int r = 0; r < RP; ++r) x[r] = a[q + r * Q];
     if constexpr (NS > 1) {
       const int bm = b & (NS - 1);
+      const float2* __restrict__ tp = tw + tw_offset(NS) + bm;
 #pragma unroll
       for (int r = 1; r < RP; ++r) {
-        float2 w = __ldg(&tw[bm * r * TWS]);
+        float2 w = __ldg(tp + r * NS);
         if (INV) w.y = -w.y;
         x[r] = cmul(x[r], w);
       }

@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(1024) k_rows_fwd(const float* __restrict__ rhs
   rows_fwd_body<N>(rhs, spec, tw);
 }
 template <int N>
-__global__ void __launch_bounds__(512) k_cols(float2* __restrict__ spec, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(512, 2) k_cols(float2* __restrict__ spec, const float2* __restrict__ tw,
                                               const float* __restrict__ k2, float scale) {
   cols_body<N>(spec, tw, k2, scale);
 }
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(1024) k_rows_fwd_b(const SolveDev* __restrict_
   rows_fwd_body<N>(f.rhs, f.spec, tw);
 }
 template <int N>
-__global__ void __launch_bounds__(512) k_cols_b(const SolveDev* __restrict__ sv, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(512, 2) k_cols_b(const SolveDev* __restrict__ sv, const float2* __restrict__ tw,
                                                 const float* __restrict__ k2, float scale) {
   cols_body<N>(sv[blockIdx.y].fft.spec, tw, k2, scale);
 }

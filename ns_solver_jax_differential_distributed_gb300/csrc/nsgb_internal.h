@@ -14,7 +14,7 @@ struct FftLaunch {
   float2* spec = nullptr;      // transposed half spectrum, (N/2 + 1) x N complex
   bool do_cols = true;         // column transform + Poisson multiplier
   float* p = nullptr;          // rows inverse output (nullptr: skip the pass)
-  const float2* tw = nullptr;  // twiddles W_N[m], m = 0..N-1
+  const float2* tw = nullptr;  // per-pass twiddle tables (nsgb_fft.cuh)
   const float* k2 = nullptr;   // squared wavenumbers, N entries
   float scale = 0.f;           // 1 / (2 N^2)
   int rows_per_cta = 8;        // even, power of two

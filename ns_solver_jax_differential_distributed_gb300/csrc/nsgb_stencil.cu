@@ -22,7 +22,7 @@ namespace nsgb {
 __device__ __forceinline__ float lap5(const float* s, int o, int W, const StepConsts& c) {
   const float f = s[o];
   const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
-  return fdiv(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f)), c.dx2);
+  return divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f)), c.dx2, c.rdx2);
 }
 
 // -(u . grad) field at centre o (NS_solver.py:474-477 central, :257-265 upwind).
@@ -32,12 +32,12 @@ __device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, fl
   const float f = s[o];
   const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
   if (SCHEME == NSGB_SCHEME_CENTRAL) {
-    const float gx = fdiv(fsub(right, left), c.h2);
-    const float gy = fdiv(fsub(up, down), c.h2);
+    const float gx = divc(fsub(right, left), c.h2, c.rh2);
+    const float gy = divc(fsub(up, down), c.h2, c.rh2);
     return -fadd(fmul(ux, gx), fmul(uy, gy));
   } else {
-    const float dfx = fdiv(ux >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1);
-    const float dfy = fdiv(uy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1);
+    const float dfx = divc(ux >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1, c.rh1);
+    const float dfy = divc(uy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1, c.rh1);
     return -fadd(fmul(ux, dfx), fmul(uy, dfy));
   }
 }
@@ -99,8 +99,8 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   if (has_p) {
     for2d<UH, UW>(tx, ty, [&](int r, int cc) {
       const int op = (r + 1) * PW + (cc + 1);
-      const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
-      const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
+      const float px = divc(fsub(sP[op + PW], sP[op - PW]), c.h2, c.rh2);
+      const float py = divc(fsub(sP[op + 1], sP[op - 1]), c.h2, c.rh2);
       const int ou = r * UW + cc;
       sUx[ou] = fsub(sUx[ou], fmul(c.dt, px));
       sUy[ou] = fsub(sUy[ou], fmul(c.dt, py));
@@ -150,9 +150,9 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
       uso[g] = sSx[o];
       uso[NN + g] = sSy[o];
-      const float gx = fdiv(fsub(sSx[o + SW], sSx[o - SW]), c.h2);
-      const float gy = fdiv(fsub(sSy[o + 1], sSy[o - 1]), c.h2);
-      rhs[g] = fdiv(fadd(gx, gy), c.dt);
+      const float gx = divc(fsub(sSx[o + SW], sSx[o - SW]), c.h2, c.rh2);
+      const float gy = divc(fsub(sSy[o + 1], sSy[o - 1]), c.h2, c.rh2);
+      rhs[g] = divc(fadd(gx, gy), c.dt, c.rdt);
     });
   }
 
@@ -268,10 +268,10 @@ __global__ void k_project(const float* __restrict__ us, const float* __restrict_
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
-  const float px = fdiv(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
-                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2);
-  const float py = fdiv(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
-                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2);
+  const float px = divc(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
+                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2);
+  const float py = divc(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
+                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2);
   u[g] = fsub(__ldg(us + g), fmul(c.dt, px));
   u[NN + g] = fsub(__ldg(us + NN + g), fmul(c.dt, py));
 }
@@ -293,10 +293,10 @@ __global__ void k_project_batch(const SolveDev* __restrict__ solves, int variant
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
   const float* p = a.p;
-  const float px = fdiv(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
-                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2);
-  const float py = fdiv(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
-                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2);
+  const float px = divc(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
+                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2);
+  const float py = divc(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
+                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2);
   d.u_final[g] = fsub(__ldg(a.us + g), fmul(c.dt, px));
   d.u_final[NN + g] = fsub(__ldg(a.us + NN + g), fmul(c.dt, py));
 }
@@ -401,8 +401,8 @@ __global__ void k_grad(const float* __restrict__ f, float* __restrict__ gx, floa
   int i, j;
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
-  gx[g] = fdiv(fsub(f[(size_t)((i + 1) & M) * N + j], f[(size_t)((i - 1) & M) * N + j]), c.h2);
-  gy[g] = fdiv(fsub(f[(size_t)i * N + ((j + 1) & M)], f[(size_t)i * N + ((j - 1) & M)]), c.h2);
+  gx[g] = divc(fsub(f[(size_t)((i + 1) & M) * N + j], f[(size_t)((i - 1) & M) * N + j]), c.h2, c.rh2);
+  gy[g] = divc(fsub(f[(size_t)i * N + ((j + 1) & M)], f[(size_t)i * N + ((j - 1) & M)]), c.h2, c.rh2);
 }
 
 __global__ void k_laplacian(const float* __restrict__ f, float* __restrict__ out, const StepConsts c) {
@@ -414,7 +414,7 @@ __global__ void k_laplacian(const float* __restrict__ f, float* __restrict__ out
   const int N = c.N, M = N - 1;
   const float left = f[(size_t)((i - 1) & M) * N + j], right = f[(size_t)((i + 1) & M) * N + j];
   const float up = f[(size_t)i * N + ((j + 1) & M)], down = f[(size_t)i * N + ((j - 1) & M)];
-  out[g] = fdiv(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f[g])), c.dx2);
+  out[g] = divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f[g])), c.dx2, c.rdx2);
 }
 
 __global__ void k_divergence(const float* __restrict__ u, float* __restrict__ out, const StepConsts c) {
@@ -425,8 +425,8 @@ __global__ void k_divergence(const float* __restrict__ u, float* __restrict__ ou
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
   const float* uy = u + NN;
-  const float gx = fdiv(fsub(u[(size_t)((i + 1) & M) * N + j], u[(size_t)((i - 1) & M) * N + j]), c.h2);
-  const float gy = fdiv(fsub(uy[(size_t)i * N + ((j + 1) & M)], uy[(size_t)i * N + ((j - 1) & M)]), c.h2);
+  const float gx = divc(fsub(u[(size_t)((i + 1) & M) * N + j], u[(size_t)((i - 1) & M) * N + j]), c.h2, c.rh2);
+  const float gy = divc(fsub(uy[(size_t)i * N + ((j + 1) & M)], uy[(size_t)i * N + ((j - 1) & M)]), c.h2, c.rh2);
   out[g] = fadd(gx, gy);
 }
 
@@ -444,12 +444,12 @@ __global__ void k_advect(const float* __restrict__ fld, const float* __restrict_
   const float up = fld[(size_t)i * N + ((j + 1) & M)], down = fld[(size_t)i * N + ((j - 1) & M)];
   const float vx = ux[g], vy = uy[g];
   if (SCHEME == NSGB_SCHEME_CENTRAL) {
-    const float gx = fdiv(fsub(right, left), c.h2);
-    const float gy = fdiv(fsub(up, down), c.h2);
+    const float gx = divc(fsub(right, left), c.h2, c.rh2);
+    const float gy = divc(fsub(up, down), c.h2, c.rh2);
     out[g] = -fadd(fmul(vx, gx), fmul(vy, gy));
   } else {
-    const float dfx = fdiv(vx >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1);
-    const float dfy = fdiv(vy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1);
+    const float dfx = divc(vx >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1, c.rh1);
+    const float dfy = divc(vy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1, c.rh1);
     out[g] = -fadd(fmul(vx, dfx), fmul(vy, dfy));
   }
 }
