@@ -82,20 +82,16 @@ struct nsgb_plan {
 
 namespace {
 
+// Launch shapes measured best on GB300 by the autotuner (see autotune.py);
+// the autotuner refines them per process.
 void default_tiles(int N, int out[4]) {
-  const int T = N / (N < 16 ? N : 16);
   out[0] = N < 64 ? N : 64;
-  out[1] = N < 16 ? N : 16;
-  int rows;
-  if (N >= 2048) rows = 8;
-  else if (N >= 512) rows = 2;
-  else if (N >= 128) rows = 4;
-  else rows = 8;
+  out[1] = N < 16 ? N : (N >= 1024 ? 16 : 8);
+  if (N <= 512 && N >= 64) out[0] = 32;
+  int rows = N >= 1024 ? 4 : (N >= 256 ? 8 : 16);
   if (rows > N) rows = N;
   out[2] = rows;
-  int kb = 512 / T;
-  if (kb < 1) kb = 1;
-  if (N >= 512 && N <= 1024) kb = 2;
+  int kb = N >= 1024 ? 1 : 4;
   if (kb > N / 2) kb = N / 2;
   out[3] = kb;
 }
