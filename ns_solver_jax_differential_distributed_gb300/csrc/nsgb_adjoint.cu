@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   const size_t NN = (size_t)N * N;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * 32 + tx;
   constexpr int PW = TW + 6, PH = TH + 6;
   constexpr int UW = TW + 4, UH = TH + 4;
   constexpr int SW = TW + 2, SH = TH + 2;
@@ -58,14 +59,14 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   const bool has_p = a.p != nullptr;
   if (has_p) {
     const float* __restrict__ pp = a.p;
-    for2d<PH, PW>(tx, ty, [&](int r, int cc) {
+    forflat<PH, PW>(tid, [&](int r, int cc) {
       sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
     });
   }
   {
     const float* __restrict__ u = a.u;
     const float* __restrict__ lam = a.lam;
-    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+    forflat<UH, UW>(tid, [&](int r, int cc) {
       const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
       const int o = r * UW + cc;
       sUx[o] = __ldg(u + g);
@@ -75,7 +76,6 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     });
   }
   {
-    const int tid = ty * 32 + tx;
     const ForcingRow fr = forcing_time(A, B, t, c);
     if (tid < SH) {
       sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   __syncthreads();
 
   if (has_p) {  // mu = lambda - dt grad p
-    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+    forflat<UH, UW>(tid, [&](int r, int cc) {
       const int op = (r + 1) * PW + (cc + 1);
       const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
       const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   // theta sensitivities on the interior cells, accumulated in double: the
   // nu term is a small difference of large contributions
   double gA = 0.0, gB = 0.0, gN = 0.0;
-  for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+  forflat<TH, TW>(tid, [&](int r, int cc) {
     const int o = (r + 2) * UW + (cc + 2);
     const float w = jscale * sUx[o] + dt * sMx[o];
     gA += (double)(w * sDA[r]);
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   // lambda_s on the tile + 1 halo
   const float inv_h2 = 1.0f / c.h2;
   const float inv_h1 = 1.0f / c.h1;
-  for2d<SH, SW>(tx, ty, [&](int r, int cc) {
+  forflat<SH, SW>(tid, [&](int r, int cc) {
     const int o = (r + 1) * UW + (cc + 1);
     const int n = o + UW, s = o - UW, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
     const float mx = sMx[o], my = sMy[o];
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   {
     float* __restrict__ lo = a.lam_out;
     float* __restrict__ rhs = a.rhs;
-    for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+    forflat<TH, TW>(tid, [&](int r, int cc) {
       const int o = (r + 1) * SW + (cc + 1);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
       lo[g] = sLx[o];

@@ -112,6 +112,23 @@ __device__ __forceinline__ void for2d(int tx, int ty, F&& f) {
   }
 }
 
+// Visit the cells (r, cc) of an H x W tile with the 256 threads of a block,
+// flattened row-major so every lane has work (rows wider than a warp would
+// otherwise leave most lanes idle in their last sweep); trip counts are
+// compile-time, so the loop unrolls and W is a constant divisor.
+template <int H, int W, class F>
+__device__ __forceinline__ void forflat(int tid, F&& f) {
+  constexpr int TOT = H * W;
+#pragma unroll
+  for (int e0 = 0; e0 < TOT; e0 += 256) {
+    const int e = e0 + tid;
+    if (TOT % 256 == 0 || e < TOT) {
+      const int r = e / W;
+      f(r, e - r * W);
+    }
+  }
+}
+
 // Stencil tile shapes (width x height) the kernels are instantiated for.
 #define NSGB_STENCIL_TILES(X) X(16, 8) X(16, 16) X(32, 8) X(32, 16) X(64, 8) X(64, 16) X(128, 8)
 

@@ -8,9 +8,9 @@
 //
 // The transform is the radix-16 Stockham autosort algorithm (a final pass of
 // radix 2/4/8 when log2(N) is not a multiple of 4).  Between passes the values
-// are exchanged through shared memory, split into real and imaginary planes
-// and padded by one word every 16 (index i -> i + i/16), which makes the pass
-// writes bank-conflict free.  Twiddles come from per-pass tables computed on
+// are exchanged through shared memory as float2, padded by one element every
+// 16 (index i -> i + i/16), which keeps the 64-bit pass writes and reads
+// bank-conflict free within each half warp.  Twiddles come from per-pass tables computed on
 // the host in double precision and rounded to float: the pass with stride NS
 // and radix RP stores W_{NS*RP}^{bm*r} at [r*NS + bm], so the twiddle loads of
 // a warp (consecutive bm) are contiguous.
@@ -111,8 +111,7 @@ __host__ __device__ constexpr int tw_entries(int N) {
 
 // One Stockham pass (stride NS) and, recursively, the remaining passes.
 template <int N, int NS, bool INV>
-__device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sre,
-                                     float* __restrict__ sim, int j,
+__device__ __forceinline__ void pass(float2 (&a)[ept(N)], float2* __restrict__ sb, int j,
                                      const float2* __restrict__ tw) {
   constexpr int E = ept(N);
   constexpr int T = N / E;
@@ -143,22 +142,15 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sr
     } else {
       const int base = (b / NS) * (NS * RP) + (b & (NS - 1));
 #pragma unroll
-      for (int r = 0; r < RP; ++r) {
-        const int idx = pad(base + r * NS);
-        sre[idx] = x[r].x;
-        sim[idx] = x[r].y;
-      }
+      for (int r = 0; r < RP; ++r) sb[pad(base + r * NS)] = x[r];
     }
   }
   if constexpr (!LAST) {
     __syncthreads();
 #pragma unroll
-    for (int s = 0; s < E; ++s) {
-      const int idx = pad(j + s * T);
-      a[s] = make_float2(sre[idx], sim[idx]);
-    }
+    for (int s = 0; s < E; ++s) a[s] = sb[pad(j + s * T)];
     __syncthreads();
-    pass<N, NS * RP, INV>(a, sre, sim, j, tw);
+    pass<N, NS * RP, INV>(a, sb, j, tw);
   }
 }
 
@@ -167,9 +159,9 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float* __restrict__ sr
 // On return the exchange buffer is free for reuse without a further barrier
 // only after the caller's next __syncthreads.
 template <int N, bool INV>
-__device__ __forceinline__ void block_fft(float2 (&a)[ept(N)], float* sre, float* sim, int j,
+__device__ __forceinline__ void block_fft(float2 (&a)[ept(N)], float2* sb, int j,
                                           const float2* __restrict__ tw) {
-  pass<N, 1, INV>(a, sre, sim, j, tw);
+  pass<N, 1, INV>(a, sb, j, tw);
 }
 
 }  // namespace fft

@@ -27,11 +27,11 @@ using fft::ept;
 using fft::pad;
 using fft::padlen;
 
-// Per-pair exchange buffer stride in floats (re plane + im plane + a small
-// skew so the buffers of different pairs start in different banks).
+// Per-transform exchange buffer stride in float2 (padded length plus a small
+// skew so the buffers of different transforms start in different banks).
 template <int N>
 __host__ __device__ constexpr int pair_stride() {
-  return 2 * padlen(N) + 4;
+  return padlen(N) + 2;
 }
 
 // ---------------------------------------------------------------- rows fwd --
@@ -42,11 +42,9 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
-  constexpr int PL = padlen(N);
-  extern __shared__ float smem[];
+  extern __shared__ float2 smem2[];
   const int j = threadIdx.x, pp = threadIdx.y, P = blockDim.y;
-  float* sre = smem + pp * pair_stride<N>();
-  float* sim = sre + PL;
+  float2* sb = smem2 + pp * pair_stride<N>();
   const int RB = 2 * P;
   const int i0 = blockIdx.x * RB;
   const float* ra = rhs + (size_t)(i0 + 2 * pp) * N;
@@ -55,14 +53,10 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) a[s] = make_float2(__ldg(ra + j + s * T), __ldg(rb + j + s * T));
-  fft::block_fft<N, false>(a, sre, sim, j, tw);
+  fft::block_fft<N, false>(a, sb, j, tw);
   __syncthreads();
 #pragma unroll
-  for (int s = 0; s < E; ++s) {
-    const int idx = pad(j + s * T);
-    sre[idx] = a[s].x;
-    sim[idx] = a[s].y;
-  }
+  for (int s = 0; s < E; ++s) sb[pad(j + s * T)] = a[s];
   __syncthreads();
 
   const int tid = threadIdx.y * T + threadIdx.x;
@@ -70,11 +64,10 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   for (int e = tid; e < RB * (H + 1); e += nth) {
     const int r = e & (RB - 1);
     const int k = e / RB;
-    const float* pre = smem + (r >> 1) * pair_stride<N>();
-    const float* pim = pre + PL;
+    const float2* pb = smem2 + (r >> 1) * pair_stride<N>();
     const int kn = (N - k) & (N - 1);
-    const float zr = pre[pad(k)], zi = pim[pad(k)];
-    const float wr = pre[pad(kn)], wi = pim[pad(kn)];
+    const float2 zk = pb[pad(k)], wk = pb[pad(kn)];
+    const float zr = zk.x, zi = zk.y, wr = wk.x, wi = wk.y;
     // 2 X_a[k] = Z[k] + conj(Z[N-k]);  2 X_b[k] = -i (Z[k] - conj(Z[N-k]))
     const float2 out = (r & 1) ? make_float2(zi + wi, wr - zr) : make_float2(zr + wr, zi - wi);
     spec[(size_t)k * N + i0 + r] = out;
@@ -96,11 +89,9 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
-  constexpr int PL = padlen(N);
-  extern __shared__ float smem[];
+  extern __shared__ float2 smem2[];
   const int j = threadIdx.x, y = threadIdx.y;
-  float* sre = smem + y * pair_stride<N>();
-  float* sim = sre + PL;
+  float2* sb = smem2 + y * pair_stride<N>();
   // N/2 + 1 rows; the last CTA may hold rows past N/2, which recompute row
   // N/2 and do not store.
   const int kreq = blockIdx.x * blockDim.y + y;
@@ -110,7 +101,7 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) a[s] = row[j + s * T];
-  fft::block_fft<N, false>(a, sre, sim, j, tw);
+  fft::block_fft<N, false>(a, sb, j, tw);
 
   const float k2y = __ldg(k2 + ky);
 #pragma unroll
@@ -118,7 +109,7 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
     const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
     a[s] = make_float2(a[s].x * g, a[s].y * g);
   }
-  fft::block_fft<N, true>(a, sre, sim, j, tw);
+  fft::block_fft<N, true>(a, sb, j, tw);
   __syncthreads();  // rows clamped to N/2 were loaded by other threads
   if (kreq <= H) {
 #pragma unroll
@@ -133,8 +124,7 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
-  constexpr int PL = padlen(N);
-  extern __shared__ float smem[];
+  extern __shared__ float2 smem2[];
   const int j = threadIdx.x, pp = threadIdx.y, P = blockDim.y;
   const int RB = 2 * P;
   const int i0 = blockIdx.x * RB;
@@ -147,15 +137,11 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     const int r = e & (RB - 1);
     const int k = e / RB;
     const float2 v = __ldg(spec + (size_t)k * N + i0 + r);
-    float* pre = smem + (r >> 1) * pair_stride<N>();
-    const int idx = pad((r & 1) * (H + 1) + k);
-    pre[idx] = v.x;
-    pre[PL + idx] = v.y;
+    smem2[(r >> 1) * pair_stride<N>() + pad((r & 1) * (H + 1) + k)] = v;
   }
   __syncthreads();
 
-  float* sre = smem + pp * pair_stride<N>();
-  float* sim = sre + PL;
+  float2* sb = smem2 + pp * pair_stride<N>();
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) {
@@ -164,20 +150,20 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     if (m == 0 || m == H) {
       // DC and Nyquist of a real row are real: their imaginary parts (rounding
       // noise of the column pass) are dropped, as Re(ifft2) drops them.
-      z = make_float2(sre[pad(m)], sre[pad(H + 1 + m)]);
+      z = make_float2(sb[pad(m)].x, sb[pad(H + 1 + m)].x);
     } else if (m < H) {
-      const float2 xa = make_float2(sre[pad(m)], sim[pad(m)]);
-      const float2 xb = make_float2(sre[pad(H + 1 + m)], sim[pad(H + 1 + m)]);
+      const float2 xa = sb[pad(m)];
+      const float2 xb = sb[pad(H + 1 + m)];
       z = make_float2(xa.x - xb.y, xa.y + xb.x);  // X_a + i X_b
     } else {
-      const float2 xa = make_float2(sre[pad(N - m)], sim[pad(N - m)]);
-      const float2 xb = make_float2(sre[pad(H + 1 + N - m)], sim[pad(H + 1 + N - m)]);
+      const float2 xa = sb[pad(N - m)];
+      const float2 xb = sb[pad(H + 1 + N - m)];
       z = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj(X_a) + i conj(X_b)
     }
     a[s] = z;
   }
   __syncthreads();
-  fft::block_fft<N, true>(a, sre, sim, j, tw);
+  fft::block_fft<N, true>(a, sb, j, tw);
   float* ra = p + (size_t)(i0 + 2 * pp) * N;
   float* rb = ra + N;
 #pragma unroll
@@ -228,8 +214,8 @@ static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, in
   constexpr int T = N / ept(N);
   const int P = L.rows_per_cta / 2;
   const int KB = L.cols_per_cta;
-  const size_t smem_rows = (size_t)P * pair_stride<N>() * sizeof(float);
-  const size_t smem_cols = (size_t)KB * pair_stride<N>() * sizeof(float);
+  const size_t smem_rows = (size_t)P * pair_stride<N>() * sizeof(float2);
+  const size_t smem_cols = (size_t)KB * pair_stride<N>() * sizeof(float2);
   static bool configured = false;  // per-process attribute set-up (idempotent)
   if (!configured) {
     const int mx = 200 * 1024;
@@ -261,10 +247,10 @@ static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, in
 }
 
 size_t fft_rows_smem_bytes(int N, int rows_per_cta) {
-  return (size_t)(rows_per_cta / 2) * (2 * padlen(N) + 4) * sizeof(float);
+  return (size_t)(rows_per_cta / 2) * (padlen(N) + 2) * sizeof(float2);
 }
 size_t fft_cols_smem_bytes(int N, int cols_per_cta) {
-  return (size_t)cols_per_cta * (2 * padlen(N) + 4) * sizeof(float);
+  return (size_t)cols_per_cta * (padlen(N) + 2) * sizeof(float2);
 }
 
 static cudaError_t dispatch(int N, const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {

@@ -50,6 +50,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   const size_t NN = (size_t)N * N;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
   const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * 32 + tx;
   constexpr int PW = TW + 6, PH = TH + 6;
   constexpr int UW = TW + 4, UH = TH + 4;
   constexpr int SW = TW + 2, SH = TH + 2;
@@ -74,20 +75,19 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   const bool has_p = a.p != nullptr;
   if (has_p) {
     const float* __restrict__ pp = a.p;
-    for2d<PH, PW>(tx, ty, [&](int r, int cc) {
+    forflat<PH, PW>(tid, [&](int r, int cc) {
       sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
     });
   }
   {
     const float* __restrict__ us = a.us;
-    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+    forflat<UH, UW>(tid, [&](int r, int cc) {
       const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
       sUx[r * UW + cc] = __ldg(us + g);
       sUy[r * UW + cc] = __ldg(us + NN + g);
     });
   }
   if (MODE == MODE_ROLLOUT) {
-    const int tid = ty * 32 + tx;
     if (tid < SH) {
       const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t, c);
       sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
@@ -97,7 +97,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
 
   // 1. pending projection u^n = u* - dt * grad p
   if (has_p) {
-    for2d<UH, UW>(tx, ty, [&](int r, int cc) {
+    forflat<UH, UW>(tid, [&](int r, int cc) {
       const int op = (r + 1) * PW + (cc + 1);
       const float px = divc(fsub(sP[op + PW], sP[op - PW]), c.h2, c.rh2);
       const float py = divc(fsub(sP[op + 1], sP[op - 1]), c.h2, c.rh2);
@@ -110,7 +110,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
 
   // 2. objective partial on the state before the step; optional state output
   float jacc = 0.0f;
-  for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+  forflat<TH, TW>(tid, [&](int r, int cc) {
     const int ou = (r + 2) * UW + (cc + 2);
     if (MODE == MODE_ROLLOUT) jacc += sUx[ou] * sF[r + 1];
     if (a.u_out) {
@@ -121,7 +121,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   });
 
   // 3. u*^{n+1} on the tile + 1 halo
-  for2d<SH, SW>(tx, ty, [&](int r, int cc) {
+  forflat<SH, SW>(tid, [&](int r, int cc) {
     const int o = (r + 1) * UW + (cc + 1);
     const float ux = sUx[o], uy = sUy[o];
     const float lapx = lap5(sUx, o, UW, c), lapy = lap5(sUy, o, UW, c);
@@ -145,7 +145,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   {
     float* __restrict__ uso = a.us_out;
     float* __restrict__ rhs = a.rhs;
-    for2d<TH, TW>(tx, ty, [&](int r, int cc) {
+    forflat<TH, TW>(tid, [&](int r, int cc) {
       const int o = (r + 1) * SW + (cc + 1);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
       uso[g] = sSx[o];
