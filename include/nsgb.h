@@ -11,6 +11,9 @@
  *    axis 2 = y (contiguous, index j) -- the reference's layout
  *    (NS_solver.py:116, 676-679).
  *  - N is a power of two, 16 <= N <= 4096.
+ *  - Fields read by the step kernels (u, u0) must be 16-byte aligned (the
+ *    kernels load them as float4 groups); a misaligned pointer is rejected
+ *    with NSGB_ERR_INVALID_ARG.
  *  - `stream` is a cudaStream_t (NULL = legacy default stream).  All calls are
  *    asynchronous with respect to the host unless stated otherwise.
  *  - Every call returns an int status (NSGB_OK = 0); on failure the

@@ -198,7 +198,10 @@ def _cuda_f32(t: torch.Tensor, name: str) -> torch.Tensor:
         raise RuntimeError(f"{name} must be a CUDA tensor (no CPU path), got {t.device}")
     if t.dtype != torch.float32:
         raise TypeError(f"{name} must be float32, got {t.dtype}")
-    return t.contiguous()
+    t = t.contiguous()
+    if t.data_ptr() % 16:
+        t = t.clone()  # the kernels read fields as aligned float4 groups
+    return t
 
 
 def _square(t: torch.Tensor, name: str, comps: int = 0) -> int:

@@ -260,6 +260,13 @@ int check_ws(void* ws, size_t have, size_t need) {
   return NSGB_OK;
 }
 
+// The stencil kernels read fields as aligned float4 groups.
+int check_field(const float* f, const char* name) {
+  if (!f) return fail(NSGB_ERR_INVALID_ARG, "%s is NULL", name);
+  if (((uintptr_t)f & 15) != 0) return fail(NSGB_ERR_INVALID_ARG, "%s must be 16-byte aligned", name);
+  return NSGB_OK;
+}
+
 int check_theta(const float* theta, int theta_len) {
   if (!theta) return fail(NSGB_ERR_INVALID_ARG, "theta is NULL");
   if (theta_len != 2 && theta_len != 3)
@@ -346,6 +353,7 @@ int check_members(const nsgb_member* members, int count, bool need_state_size) {
       return fail(NSGB_ERR_INVALID_ARG, "member %d: phys.L differs from its plan's L", i);
     if (int r = check_theta(m.theta, m.theta_len)) return r;
     if (!m.u0 || !m.u_final || !m.J) return fail(NSGB_ERR_INVALID_ARG, "member %d: NULL pointer", i);
+    if (int r = check_field(m.u0, "member u0")) return r;
     if (m.total_steps < 1) return fail(NSGB_ERR_INVALID_ARG, "member %d: total_steps must be >= 1", i);
     if (m.done_steps < 0 || m.done_steps > m.total_steps)
       return fail(NSGB_ERR_INVALID_ARG, "member %d: done_steps out of range", i);
@@ -659,6 +667,7 @@ int nsgb_projector_step(const nsgb_plan* plan, const nsgb_phys* phys, const floa
   if (int r = check_plan(plan)) return r;
   if (int r = check_phys(phys)) return r;
   if (!u || !f || !u_out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
+  if (int r = check_field(u, "u")) return r;
   RolloutWs w = carve_rollout(plan, 1, nullptr);
   if (int r = check_ws(workspace, ws_bytes, w.bytes)) return r;
   w = carve_rollout(plan, 1, workspace);
@@ -682,6 +691,7 @@ int nsgb_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, cons
   if (int r = check_phys(phys)) return r;
   if (int r = check_theta(theta, theta_len)) return r;
   if (!u || !u_out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
+  if (int r = check_field(u, "u")) return r;
   RolloutWs w = carve_rollout(plan, 1, nullptr);
   if (int r = check_ws(workspace, ws_bytes, w.bytes)) return r;
   w = carve_rollout(plan, 1, workspace);
@@ -712,6 +722,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
   if (int r = check_phys(phys)) return r;
   if (int r = check_theta(theta, theta_len)) return r;
   if (!u0 || !u_final || !J) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
+  if (int r = check_field(u0, "u0")) return r;
   if (steps < 0) return fail(NSGB_ERR_INVALID_ARG, "steps must be >= 0");
   const size_t need = carve_rollout(plan, steps, nullptr).bytes;
   if (int r = check_ws(workspace, ws_bytes, need)) return r;
@@ -818,7 +829,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   if (int r = check_plan(plan)) return r;
   if (int r = check_phys(phys)) return r;
   if (int r = check_theta(theta, theta_len)) return r;
-  if (!u0) return fail(NSGB_ERR_INVALID_ARG, "u0 is NULL");
+  if (int r = check_field(u0, "u0")) return r;
   if (steps < 1) return fail(NSGB_ERR_INVALID_ARG, "steps must be >= 1");
   if (every < 1) return fail(NSGB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
   if (phases < 1 || phases > 3) return fail(NSGB_ERR_INVALID_ARG, "phases must be 1, 2 or 3");
@@ -1033,6 +1044,7 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
   if (int r = check_phys(phys)) return r;
   if (int r = check_theta(theta, theta_len)) return r;
   if (!u0 || !out_ms) return fail(NSGB_ERR_INVALID_ARG, "NULL pointer");
+  if (int r = check_field(u0, "u0")) return r;
   if (reps < 1) return fail(NSGB_ERR_INVALID_ARG, "reps must be >= 1");
   const size_t need = carve_rollout(plan, 1, nullptr).bytes;
   if (int r = check_ws(workspace, ws_bytes, need)) return r;

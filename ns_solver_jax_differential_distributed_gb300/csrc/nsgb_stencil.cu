@@ -18,19 +18,18 @@
 
 namespace nsgb {
 
-// 5-point Laplacian at centre o of a tile with row pitch W (NS_solver.py:249-255).
-__device__ __forceinline__ float lap5(const float* s, int o, int W, const StepConsts& c) {
-  const float f = s[o];
-  const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
+// 5-point Laplacian from the centre value and its four neighbours
+// (left/right = i -+ 1, down/up = j -+ 1; NS_solver.py:249-255).
+__device__ __forceinline__ float lap5(float f, float left, float right, float up, float down,
+                                      const StepConsts& c) {
   return divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f)), c.dx2, c.rdx2);
 }
 
-// -(u . grad) field at centre o (NS_solver.py:474-477 central, :257-265 upwind).
+// -(u . grad) f from the same five values (NS_solver.py:474-477 central,
+// :257-265 upwind).
 template <int SCHEME>
-__device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, float uy,
-                                      const StepConsts& c) {
-  const float f = s[o];
-  const float left = s[o - W], right = s[o + W], up = s[o + 1], down = s[o - 1];
+__device__ __forceinline__ float adv5(float f, float left, float right, float up, float down, float ux,
+                                      float uy, const StepConsts& c) {
   if (SCHEME == NSGB_SCHEME_CENTRAL) {
     const float gx = divc(fsub(right, left), c.h2, c.rh2);
     const float gy = divc(fsub(up, down), c.h2, c.rh2);
@@ -42,25 +41,39 @@ __device__ __forceinline__ float adv5(const float* s, int o, int W, float ux, fl
   }
 }
 
+// Shared-memory layout of one TW x TH tile (TW a multiple of 4).  Tiles are
+// fetched from HBM as aligned float4 groups covering columns j0-4 .. j0+TW+3
+// (a 16-byte-aligned superset of the halos): the pressure as floats, the two
+// velocity components interleaved as float2 so one 64-bit shared load serves
+// both.
+template <int TW, int TH>
+struct StencilSmem {
+  static constexpr int G = TW / 4 + 2;        // float4 groups per tile row
+  static constexpr int W4 = 4 * G;            // = TW + 8 columns, from j0 - 4
+  static constexpr int PH = TH + 6, UH = TH + 4, SH = TH + 2, SW = TW + 2;
+  static constexpr int P_OFF = 0;                       // floats, PH x W4
+  static constexpr int U_OFF = P_OFF + PH * W4;         // float2, UH x W4
+  static constexpr int S_OFF = U_OFF + 2 * UH * W4;     // float2, SH x SW
+  static constexpr int F_OFF = S_OFF + 2 * SH * SW;     // floats, SH forcing rows
+  static constexpr int R_OFF = F_OFF + SH + 2;          // floats, 8 partial sums
+  static constexpr int FLOATS = R_OFF + 8;
+};
+
 template <int SCHEME, int MODE, int TW, int TH>
 __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off = 0) {
-  extern __shared__ float sm[];
+  using L = StencilSmem<TW, TH>;
+  constexpr int G = L::G, W4 = L::W4, PH = L::PH, UH = L::UH, SH = L::SH, SW = L::SW;
+  extern __shared__ __align__(16) float sm[];
+  float* sP = sm + L::P_OFF;
+  float2* sU = reinterpret_cast<float2*>(sm + L::U_OFF);
+  float2* sS = reinterpret_cast<float2*>(sm + L::S_OFF);
+  float* sF = sm + L::F_OFF;
+  float* sRed = sm + L::R_OFF;
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
   const size_t NN = (size_t)N * N;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int tid = ty * 32 + tx;
-  constexpr int PW = TW + 6, PH = TH + 6;
-  constexpr int UW = TW + 4, UH = TH + 4;
-  constexpr int SW = TW + 2, SH = TH + 2;
-  float* sP = sm;
-  float* sUx = sP + PH * PW;
-  float* sUy = sUx + UH * UW;
-  float* sSx = sUy + UH * UW;
-  float* sSy = sSx + SH * SW;
-  float* sF = sSy + SH * SW;
-  float* sRed = sF + SH;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
 
   int step = 0;
   float t = a.t_fixed;
@@ -70,40 +83,46 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   }
   const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
 
-  // Tile loads: compile-time trip counts, so every load of a thread is in
-  // flight before the first shared-memory store.
+  // Tile loads: aligned float4 groups (a group never straddles the periodic
+  // wrap because N and the group start are multiples of 4).
   const bool has_p = a.p != nullptr;
   if (has_p) {
     const float* __restrict__ pp = a.p;
-    forflat<PH, PW>(tid, [&](int r, int cc) {
-      sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
+    forflat<PH, G>(tid, [&](int r, int q) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(
+          pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M)));
+      *reinterpret_cast<float4*>(sP + r * W4 + 4 * q) = v;
     });
   }
   {
     const float* __restrict__ us = a.us;
-    forflat<UH, UW>(tid, [&](int r, int cc) {
-      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
-      sUx[r * UW + cc] = __ldg(us + g);
-      sUy[r * UW + cc] = __ldg(us + NN + g);
+    forflat<UH, G>(tid, [&](int r, int q) {
+      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 4 + 4 * q) & M);
+      const float4 x = __ldg(reinterpret_cast<const float4*>(us + g));
+      const float4 y = __ldg(reinterpret_cast<const float4*>(us + NN + g));
+      float4* dst = reinterpret_cast<float4*>(sU + r * W4 + 4 * q);
+      dst[0] = make_float4(x.x, y.x, x.y, y.y);
+      dst[1] = make_float4(x.z, y.z, x.w, y.w);
     });
   }
-  if (MODE == MODE_ROLLOUT) {
-    if (tid < SH) {
-      const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t, c);
-      sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
-    }
+  if (MODE == MODE_ROLLOUT && tid < SH) {
+    const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t, c);
+    sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
   }
   __syncthreads();
 
-  // 1. pending projection u^n = u* - dt * grad p
+  // 1. pending projection u^n = u* - dt grad p on rows i0-2.., columns
+  //    j0-2 .. j0+TW+1 (sU columns 2 .. TW+5)
   if (has_p) {
-    forflat<UH, UW>(tid, [&](int r, int cc) {
-      const int op = (r + 1) * PW + (cc + 1);
-      const float px = divc(fsub(sP[op + PW], sP[op - PW]), c.h2, c.rh2);
-      const float py = divc(fsub(sP[op + 1], sP[op - 1]), c.h2, c.rh2);
-      const int ou = r * UW + cc;
-      sUx[ou] = fsub(sUx[ou], fmul(c.dt, px));
-      sUy[ou] = fsub(sUy[ou], fmul(c.dt, py));
+    forflat<UH, TW + 4>(tid, [&](int r, int cc) {
+      const int col = cc + 2;
+      const float* P0 = sP + (r + 1) * W4 + col;  // p at (i0-2+r, j0-2+cc)
+      const float px = divc(fsub(P0[W4], P0[-W4]), c.h2, c.rh2);
+      const float py = divc(fsub(P0[1], P0[-1]), c.h2, c.rh2);
+      float2 u = sU[r * W4 + col];
+      u.x = fsub(u.x, fmul(c.dt, px));
+      u.y = fsub(u.y, fmul(c.dt, py));
+      sU[r * W4 + col] = u;
     });
     __syncthreads();
   }
@@ -111,22 +130,23 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   // 2. objective partial on the state before the step; optional state output
   float jacc = 0.0f;
   forflat<TH, TW>(tid, [&](int r, int cc) {
-    const int ou = (r + 2) * UW + (cc + 2);
-    if (MODE == MODE_ROLLOUT) jacc += sUx[ou] * sF[r + 1];
+    const float2 u = sU[(r + 2) * W4 + cc + 4];
+    if (MODE == MODE_ROLLOUT) jacc += u.x * sF[r + 1];
     if (a.u_out) {
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      a.u_out[g] = sUx[ou];
-      a.u_out[NN + g] = sUy[ou];
+      a.u_out[g] = u.x;
+      a.u_out[NN + g] = u.y;
     }
   });
 
-  // 3. u*^{n+1} on the tile + 1 halo
+  // 3. u*^{n+1} on rows i0-1 .. i0+TH, columns j0-1 .. j0+TW
   forflat<SH, SW>(tid, [&](int r, int cc) {
-    const int o = (r + 1) * UW + (cc + 1);
-    const float ux = sUx[o], uy = sUy[o];
-    const float lapx = lap5(sUx, o, UW, c), lapy = lap5(sUy, o, UW, c);
-    const float advx = adv5<SCHEME>(sUx, o, UW, ux, uy, c);
-    const float advy = adv5<SCHEME>(sUy, o, UW, ux, uy, c);
+    const float2* U0 = sU + (r + 1) * W4 + cc + 3;
+    const float2 o = U0[0], lf = U0[-W4], rt = U0[W4], up = U0[1], dn = U0[-1];
+    const float lapx = lap5(o.x, lf.x, rt.x, up.x, dn.x, c);
+    const float lapy = lap5(o.y, lf.y, rt.y, up.y, dn.y, c);
+    const float advx = adv5<SCHEME>(o.x, lf.x, rt.x, up.x, dn.x, o.x, o.y, c);
+    const float advy = adv5<SCHEME>(o.y, lf.y, rt.y, up.y, dn.y, o.x, o.y, c);
     float fx, fy;
     if (MODE == MODE_ROLLOUT) {
       fx = sF[r];
@@ -136,27 +156,29 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
       fx = __ldg(a.f + g);
       fy = __ldg(a.f + NN + g);
     }
-    sSx[r * SW + cc] = fadd(ux, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
-    sSy[r * SW + cc] = fadd(uy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+    sS[r * SW + cc] = make_float2(fadd(o.x, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx))),
+                                  fadd(o.y, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy))));
   });
   __syncthreads();
 
-  // 4. write u*^{n+1} and div(u*^{n+1}) / dt
+  // 4. write u*^{n+1} and div(u*^{n+1}) / dt for the tile
   {
     float* __restrict__ uso = a.us_out;
     float* __restrict__ rhs = a.rhs;
     forflat<TH, TW>(tid, [&](int r, int cc) {
-      const int o = (r + 1) * SW + (cc + 1);
+      const float2* S0 = sS + (r + 1) * SW + cc + 1;
+      const float2 o = S0[0];
+      const float gx = divc(fsub(S0[SW].x, S0[-SW].x), c.h2, c.rh2);
+      const float gy = divc(fsub(S0[1].y, S0[-1].y), c.h2, c.rh2);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      uso[g] = sSx[o];
-      uso[NN + g] = sSy[o];
-      const float gx = divc(fsub(sSx[o + SW], sSx[o - SW]), c.h2, c.rh2);
-      const float gy = divc(fsub(sSy[o + 1], sSy[o - 1]), c.h2, c.rh2);
+      uso[g] = o.x;
+      uso[NN + g] = o.y;
       rhs[g] = divc(fadd(gx, gy), c.dt, c.rdt);
     });
   }
 
   if (MODE == MODE_ROLLOUT) {
+    const int tx = threadIdx.x, ty = threadIdx.y;
     jacc = warp_sum(jacc);
     if (tx == 0) sRed[ty] = jacc;
     __syncthreads();
@@ -192,10 +214,9 @@ bool stencil_tile_supported(int tw, int th) {
   return false;
 }
 
-static size_t stencil_smem(int tw, int th) {
-  const size_t f = (size_t)(th + 6) * (tw + 6) + 2 * (size_t)(th + 4) * (tw + 4) +
-                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 32;
-  return f * sizeof(float);
+template <int TW, int TH>
+static constexpr size_t stencil_smem() {
+  return StencilSmem<TW, TH>::FLOATS * sizeof(float);
 }
 
 template <int SCHEME, int MODE, int TW, int TH>
@@ -207,7 +228,7 @@ static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
     configured = true;
   }
   const dim3 grid(a.c.N / TW, a.c.N / TH);
-  k_stencil<SCHEME, MODE, TW, TH><<<grid, dim3(32, 8), stencil_smem(TW, TH), st>>>(a);
+  k_stencil<SCHEME, MODE, TW, TH><<<grid, dim3(32, 8), stencil_smem<TW, TH>(), st>>>(a);
   return cudaGetLastError();
 }
 
@@ -221,7 +242,8 @@ static cudaError_t launch_stencil_batch_t(const SolveDev* solves, int count, int
     configured = true;
   }
   const dim3 grid(N / TW, N / TH, count);
-  k_stencil_batch<SCHEME, TW, TH><<<grid, dim3(32, 8), stencil_smem(TW, TH), st>>>(solves, variant, step_off);
+  k_stencil_batch<SCHEME, TW, TH><<<grid, dim3(32, 8), stencil_smem<TW, TH>(), st>>>(solves, variant,
+                                                                                   step_off);
   return cudaGetLastError();
 }
 
