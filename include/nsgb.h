@@ -208,6 +208,27 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
                      size_t flush_bytes, void* workspace, size_t workspace_bytes, float* out_ms,
                      void* stream);
 
+/* Largest N accepted by nsgb_poisson_noalloc. */
+#define NSGB_NOALLOC_MAX_N 1024
+
+/* No counterpart in the reference.  The spectral Poisson solve of
+ * nsgb_poisson (lap(p) = rhs, same kernels, same results) for callers that
+ * cannot allocate device memory when they solve: code confined to a fixed
+ * device-memory budget it cannot grow, loops in which a cudaMalloc (which may
+ * synchronise the device) is unacceptable, and plain C FFI hosts that cannot
+ * own a plan and a workspace.  It needs no plan and no workspace: its scratch
+ * (the half spectrum and the constant tables) is a file-scope static device
+ * array for N <= NSGB_NOALLOC_MAX_N, about 4.2 MB held on every GPU that loads
+ * the library until the process exits; larger N is rejected with
+ * NSGB_ERR_UNSUPPORTED_N.  It calls no cudaMalloc or cudaFree.  The first call
+ * on a device resolves the arrays' device addresses (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture.
+ * All calls share the arrays, which keep the last call's contents: calls
+ * whose work overlaps on the GPU (other streams or host threads) race and
+ * must be serialised by the caller.  rhs and p are (N,N) float32 device
+ * fields on the current device. */
+int nsgb_poisson_noalloc(int N, double L, const float* rhs, float* p, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -491,6 +491,8 @@ cudaError_t rollout_step(const nsgb_plan* plan, StencilArgs a, const float* us_i
 
 }  // namespace
 
+void nsgb::set_last_error(const char* msg) { g_last_error = msg; }
+
 // ============================================================== C ABI ====
 extern "C" {
 

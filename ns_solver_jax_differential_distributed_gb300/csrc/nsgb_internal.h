@@ -117,4 +117,7 @@ cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
 cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
 cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st);
 
+// Record the message nsgb_last_error() returns on this host thread.
+void set_last_error(const char* msg);
+
 }  // namespace nsgb
