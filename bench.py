@@ -52,6 +52,11 @@ def parse_args(argv=None):
     ap.add_argument("--scheme", choices=["central", "upwind"], default="central")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["plain", "grad", "ensemble", "serve"], default="plain",
+                    help="plain: the headline N=4096 rollout (default); grad: N=1024 adjoint; "
+                         "ensemble: 256 uneven solves; serve: Poisson-arrival serving")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     return ap.parse_args(argv)
 
 
@@ -340,9 +345,139 @@ def run_reference(args, world, rank):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ------------------------------------------------- the systems workloads
+def run_grad(args):
+    """Differentiation: dJ/dtheta by the discrete adjoint, N=1024, 1000 steps,
+    dt=1e-3, nu=5e-4, upwind, checkpoints every 50 steps; time against the
+    forward rollout, peak memory, and central finite differences of the GPU
+    forward (relative steps 1e-4 for A, 1e-3 for B and nu)."""
+    import torch
+    import ns_solver_jax_differential_distributed_gb300 as nsgb
+    from ns_solver_jax_differential_distributed_gb300 import _build, autotune
+    from ns_solver_jax_differential_distributed_gb300.workloads import GRAD_N1024 as w, GRAD_CHECKPOINT_EVERY
+    _build.build()
+    dev = torch.device("cuda", 0)
+    autotune.tune(w.N, w.L, w.scheme, dev)
+    solver = nsgb.SingleCoreNSSolver(nsgb.make_grid(w.N, w.L), nsgb.Phys(nu=w.nu, mu0=0.5, sigma0=0.1, C=1.0),
+                                     nsgb.Time(dt=w.dt, steps=w.steps), w.scheme, device=dev,
+                                     checkpoint_every=GRAD_CHECKPOINT_EVERY)
+    u0 = torch.from_numpy(w.u0()).to(dev)
+    th = torch.from_numpy(w.theta()).to(dev)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps, out
+
+    torch.cuda.reset_peak_memory_stats(dev)
+    t_fwd, (J, _) = timed(lambda: solver.rollout(u0, th), max(1, args.steps))
+    mem_fwd = torch.cuda.max_memory_allocated(dev)
+    torch.cuda.reset_peak_memory_stats(dev)
+    t_grad, (Jg, g) = timed(lambda: solver.gradient(u0, th), max(1, args.steps))
+    mem_grad = torch.cuda.max_memory_allocated(dev)
+    g = g.double().cpu().numpy()
+    th64 = th.double().cpu().numpy()
+    fd = []
+    for k, rs in enumerate((1e-4, 1e-3, 1e-3)):
+        h = rs * abs(th64[k])
+        tp, tm = th64.copy(), th64.copy()
+        tp[k] += h
+        tm[k] -= h
+        Jp = float(solver.rollout(u0, torch.tensor(tp, dtype=torch.float32, device=dev))[0])
+        Jm = float(solver.rollout(u0, torch.tensor(tm, dtype=torch.float32, device=dev))[0])
+        fd.append((Jp - Jm) / (2 * h))
+    cells = float(w.N) * w.N * w.steps
+    return {"metric": "adjoint gradient time / forward time", "value": t_grad / t_fwd, "unit": "x",
+            "higher_is_better": False, "workload": w.name, "N": w.N, "steps": w.steps, "scheme": w.scheme,
+            "checkpoint_every": GRAD_CHECKPOINT_EVERY, "forward_ms": t_fwd, "gradient_ms": t_grad,
+            "forward_cell_steps_per_s": cells / (t_fwd / 1e3), "J": float(Jg), "dJdtheta": g.tolist(),
+            "fd_gpu_float32": fd, "fd_rel_diff": [abs(a - b) / max(abs(b), 1e-30) for a, b in zip(g, fd)],
+            "peak_mem_forward_bytes": mem_fwd, "peak_mem_gradient_bytes": mem_grad,
+            "dtype": "f32", "data": "synthetic"}
+
+
+def run_ensemble(args):
+    """Batching: 256 solves, N in {64,128,256,512} w.p. {.4,.3,.2,.1}, 500
+    steps, per-solve nu/theta/u0; one batched launch per stage per N-group,
+    CUDA-graph chunks of 16 steps; against 256 sequential plain rollouts."""
+    import torch
+    from ns_solver_jax_differential_distributed_gb300 import _build, ensemble
+    from ns_solver_jax_differential_distributed_gb300.workloads import ensemble as make_ensemble
+    _build.build()
+    dev = torch.device("cuda", 0)
+    members = make_ensemble()
+    specs = ensemble.from_workload(members)
+    ens = ensemble.Ensemble(specs, steps=members[0].steps, device=dev, chunk=16, tune=True)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(max(1, args.steps)):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / max(1, args.steps), out
+
+    t_b, (Jb, ub) = timed(ens.run)
+    Jb, ub = Jb.clone(), [u.clone() for u in ub]
+    t_s, (Js, us) = timed(ens.run_sequential)
+    same = bool(torch.equal(Jb, Js)) and all(torch.equal(a, b) for a, b in zip(ub, us))
+    cells = float(ens.cell_steps)
+    sizes = {}
+    for m in members:
+        sizes[m.N] = sizes.get(m.N, 0) + 1
+    return {"metric": "batched cell-steps/s", "value": cells / (t_b / 1e3), "unit": "cell-steps/s",
+            "sequential_cell_steps_per_s": cells / (t_s / 1e3), "speedup_vs_sequential": t_s / t_b,
+            "solves_per_s_batched": len(members) / (t_b / 1e3),
+            "solves_per_s_sequential": len(members) / (t_s / 1e3),
+            "batched_ms": t_b, "sequential_ms": t_s, "bitwise_equal_to_sequential": same,
+            "members": len(members), "sizes": sizes, "steps": members[0].steps, "dtype": "f32",
+            "data": "synthetic", "chunk": 16}
+
+
+def run_serve(args):
+    """Serving: Poisson arrivals at --rate for --duration s; N uniform over
+    {128..2048}, steps U[100,2000], 30% forward+adjoint; 150 GB HBM budget;
+    continuous batching.  Reports solves/s and p50/p99 latency; the run stops
+    30 s after the last arrival (requests still queued are reported)."""
+    import torch
+    from ns_solver_jax_differential_distributed_gb300 import _build, serve, autotune
+    _build.build()
+    dev = torch.device("cuda", 0)
+    for N in (128, 256, 512, 1024, 2048):
+        autotune.tune(N, 2 * math.pi, "central", dev)
+    reqs = serve.make_trace(rate=args.rate, duration=args.duration, seed=7)
+    srv = serve.Server(dev, hbm_budget=150e9)
+    for N in (128, 256, 512, 1024, 2048):
+        for s in range(16):
+            srv.u0.get(N, s)
+    t0 = time.perf_counter()
+    done, trace = srv.run(reqs, realtime=True, drain_limit=30.0)
+    wall = time.perf_counter() - t0
+    summ = serve.summarize(reqs, done, wall)
+    summ.update({"metric": "served solves/s", "rate_req_per_s": args.rate, "duration_s": args.duration,
+                 "max_queue": max(q[1] for q in trace) if trace else 0,
+                 "queue_at_end": trace[-1][1] if trace else 0,
+                 "grad_fraction_completed": sum(r.kind == "grad" for r in done) / max(1, len(done))})
+    return summ
+
+
 def main(argv=None):
     args = parse_args(argv)
     world, rank, local = dist_env()
+    if args.workload != "plain":
+        if rank == 0:
+            fn = {"grad": run_grad, "ensemble": run_ensemble, "serve": run_serve}[args.workload]
+            print(json.dumps(fn(args)), flush=True)
+        return
     if args.impl == "reference":
         res = run_reference(args, world, rank)
     else:

@@ -176,6 +176,7 @@ class Server:
         stream = torch.cuda.current_stream(self.device)
         completed = []
         queue_trace = []
+        ticks = collections.deque()  # events of the ticks still on the GPU
         while True:
             now = time.perf_counter() - t0
             while nxt < len(reqs) and (not realtime or reqs[nxt].arrival <= now):
@@ -238,6 +239,13 @@ class Server:
                         keep.append(a)
                 active = keep
                 self.stats["ticks"] += 1
+                # keep at most two ticks queued on the GPU, so admission and
+                # the host's view of progress follow the device
+                tev = torch.cuda.Event()
+                tev.record(stream)
+                ticks.append(tev)
+                if len(ticks) > 2:
+                    ticks.popleft().synchronize()
             # completions
             still = []
             for ev, a in finishing:
