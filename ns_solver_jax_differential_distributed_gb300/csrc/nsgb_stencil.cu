@@ -41,21 +41,23 @@ __device__ __forceinline__ float adv5(float f, float left, float right, float up
   }
 }
 
-// Shared-memory layout of one TW x TH tile (TW a multiple of 4).  Tiles are
-// fetched from HBM as aligned float4 groups covering columns j0-4 .. j0+TW+3
-// (a 16-byte-aligned superset of the halos): the pressure as floats, the two
-// velocity components interleaved as float2 so one 64-bit shared load serves
-// both.
+// Shared-memory layout of one TW x TH tile (TW a multiple of 4, TH even).
+// Tiles are fetched from HBM as aligned float4 groups covering columns
+// j0-4 .. j0+TW+3 (a 16-byte-aligned superset of the halos); each field
+// component has its own plane, so a warp's accesses along a row are
+// consecutive words.
 template <int TW, int TH>
 struct StencilSmem {
   static constexpr int G = TW / 4 + 2;        // float4 groups per tile row
   static constexpr int W4 = 4 * G;            // = TW + 8 columns, from j0 - 4
   static constexpr int PH = TH + 6, UH = TH + 4, SH = TH + 2, SW = TW + 2;
-  static constexpr int P_OFF = 0;                       // floats, PH x W4
-  static constexpr int U_OFF = P_OFF + PH * W4;         // float2, UH x W4
-  static constexpr int S_OFF = U_OFF + 2 * UH * W4;     // float2, SH x SW
-  static constexpr int F_OFF = S_OFF + 2 * SH * SW;     // floats, SH forcing rows
-  static constexpr int R_OFF = F_OFF + SH + 2;          // floats, 8 partial sums
+  static constexpr int P_OFF = 0;                     // PH x W4
+  static constexpr int UX_OFF = P_OFF + PH * W4;      // UH x W4
+  static constexpr int UY_OFF = UX_OFF + UH * W4;     // UH x W4
+  static constexpr int SX_OFF = UY_OFF + UH * W4;     // SH x SW
+  static constexpr int SY_OFF = SX_OFF + SH * SW;     // SH x SW
+  static constexpr int F_OFF = SY_OFF + SH * SW;      // SH forcing rows
+  static constexpr int R_OFF = F_OFF + SH + 2;        // 8 partial sums
   static constexpr int FLOATS = R_OFF + 8;
 };
 
@@ -63,10 +65,13 @@ template <int SCHEME, int MODE, int TW, int TH>
 __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off = 0) {
   using L = StencilSmem<TW, TH>;
   constexpr int G = L::G, W4 = L::W4, PH = L::PH, UH = L::UH, SH = L::SH, SW = L::SW;
+  static_assert(TH % 2 == 0, "the u* phase works on pairs of rows");
   extern __shared__ __align__(16) float sm[];
   float* sP = sm + L::P_OFF;
-  float2* sU = reinterpret_cast<float2*>(sm + L::U_OFF);
-  float2* sS = reinterpret_cast<float2*>(sm + L::S_OFF);
+  float* sUx = sm + L::UX_OFF;
+  float* sUy = sm + L::UY_OFF;
+  float* sSx = sm + L::SX_OFF;
+  float* sSy = sm + L::SY_OFF;
   float* sF = sm + L::F_OFF;
   float* sRed = sm + L::R_OFF;
   const StepConsts& c = a.c;
@@ -98,11 +103,8 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     const float* __restrict__ us = a.us;
     forflat<UH, G>(tid, [&](int r, int q) {
       const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 4 + 4 * q) & M);
-      const float4 x = __ldg(reinterpret_cast<const float4*>(us + g));
-      const float4 y = __ldg(reinterpret_cast<const float4*>(us + NN + g));
-      float4* dst = reinterpret_cast<float4*>(sU + r * W4 + 4 * q);
-      dst[0] = make_float4(x.x, y.x, x.y, y.y);
-      dst[1] = make_float4(x.z, y.z, x.w, y.w);
+      *reinterpret_cast<float4*>(sUx + r * W4 + 4 * q) = __ldg(reinterpret_cast<const float4*>(us + g));
+      *reinterpret_cast<float4*>(sUy + r * W4 + 4 * q) = __ldg(reinterpret_cast<const float4*>(us + NN + g));
     });
   }
   if (MODE == MODE_ROLLOUT && tid < SH) {
@@ -111,18 +113,17 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   }
   __syncthreads();
 
-  // 1. pending projection u^n = u* - dt grad p on rows i0-2.., columns
-  //    j0-2 .. j0+TW+1 (sU columns 2 .. TW+5)
+  // 1. pending projection u^n = u* - dt grad p on rows i0-2 .. i0+TH+1 and
+  //    columns j0-2 .. j0+TW+1 (plane columns 2 .. TW+5)
   if (has_p) {
     forflat<UH, TW + 4>(tid, [&](int r, int cc) {
       const int col = cc + 2;
       const float* P0 = sP + (r + 1) * W4 + col;  // p at (i0-2+r, j0-2+cc)
       const float px = divc(fsub(P0[W4], P0[-W4]), c.h2, c.rh2);
       const float py = divc(fsub(P0[1], P0[-1]), c.h2, c.rh2);
-      float2 u = sU[r * W4 + col];
-      u.x = fsub(u.x, fmul(c.dt, px));
-      u.y = fsub(u.y, fmul(c.dt, py));
-      sU[r * W4 + col] = u;
+      const int o = r * W4 + col;
+      sUx[o] = fsub(sUx[o], fmul(c.dt, px));
+      sUy[o] = fsub(sUy[o], fmul(c.dt, py));
     });
     __syncthreads();
   }
@@ -130,34 +131,50 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   // 2. objective partial on the state before the step; optional state output
   float jacc = 0.0f;
   forflat<TH, TW>(tid, [&](int r, int cc) {
-    const float2 u = sU[(r + 2) * W4 + cc + 4];
-    if (MODE == MODE_ROLLOUT) jacc += u.x * sF[r + 1];
+    const int o = (r + 2) * W4 + cc + 4;
+    if (MODE == MODE_ROLLOUT) jacc += sUx[o] * sF[r + 1];
     if (a.u_out) {
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      a.u_out[g] = u.x;
-      a.u_out[NN + g] = u.y;
+      a.u_out[g] = sUx[o];
+      a.u_out[NN + g] = sUy[o];
     }
   });
 
-  // 3. u*^{n+1} on rows i0-1 .. i0+TH, columns j0-1 .. j0+TW
-  forflat<SH, SW>(tid, [&](int r, int cc) {
-    const float2* U0 = sU + (r + 1) * W4 + cc + 3;
-    const float2 o = U0[0], lf = U0[-W4], rt = U0[W4], up = U0[1], dn = U0[-1];
-    const float lapx = lap5(o.x, lf.x, rt.x, up.x, dn.x, c);
-    const float lapy = lap5(o.y, lf.y, rt.y, up.y, dn.y, c);
-    const float advx = adv5<SCHEME>(o.x, lf.x, rt.x, up.x, dn.x, o.x, o.y, c);
-    const float advy = adv5<SCHEME>(o.y, lf.y, rt.y, up.y, dn.y, o.x, o.y, c);
-    float fx, fy;
-    if (MODE == MODE_ROLLOUT) {
-      fx = sF[r];
-      fy = 0.0f;
-    } else {
-      const size_t g = (size_t)((i0 - 1 + r) & M) * N + ((j0 - 1 + cc) & M);
-      fx = __ldg(a.f + g);
-      fy = __ldg(a.f + NN + g);
+  // 3. u*^{n+1} on rows i0-1 .. i0+TH and columns j0-1 .. j0+TW, two
+  //    vertically adjacent cells per thread (rows 2h and 2h+1 of the S tile)
+  //    sharing their column loads
+  forflat<SH / 2, SW>(tid, [&](int h, int cc) {
+    const int r = 2 * h;
+    const int o = (r + 1) * W4 + cc + 3;  // U cell of S cell (r, cc)
+    float x[4], y[4];                     // U rows r .. r+3 at the cell's column
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      x[k] = sUx[o + (k - 1) * W4];
+      y[k] = sUy[o + (k - 1) * W4];
     }
-    sS[r * SW + cc] = make_float2(fadd(o.x, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx))),
-                                  fadd(o.y, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy))));
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const int ok = o + k * W4;
+      const float ox = x[k + 1], oy = y[k + 1];
+      const float lx = x[k], rx = x[k + 2], ux_ = sUx[ok + 1], dx_ = sUx[ok - 1];
+      const float ly = y[k], ry = y[k + 2], uy_ = sUy[ok + 1], dy_ = sUy[ok - 1];
+      const float lapx = lap5(ox, lx, rx, ux_, dx_, c);
+      const float lapy = lap5(oy, ly, ry, uy_, dy_, c);
+      const float advx = adv5<SCHEME>(ox, lx, rx, ux_, dx_, ox, oy, c);
+      const float advy = adv5<SCHEME>(oy, ly, ry, uy_, dy_, ox, oy, c);
+      float fx, fy;
+      if (MODE == MODE_ROLLOUT) {
+        fx = sF[r + k];
+        fy = 0.0f;
+      } else {
+        const size_t g = (size_t)((i0 - 1 + r + k) & M) * N + ((j0 - 1 + cc) & M);
+        fx = __ldg(a.f + g);
+        fy = __ldg(a.f + NN + g);
+      }
+      const int so = (r + k) * SW + cc;
+      sSx[so] = fadd(ox, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
+      sSy[so] = fadd(oy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+    }
   });
   __syncthreads();
 
@@ -166,13 +183,12 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     float* __restrict__ uso = a.us_out;
     float* __restrict__ rhs = a.rhs;
     forflat<TH, TW>(tid, [&](int r, int cc) {
-      const float2* S0 = sS + (r + 1) * SW + cc + 1;
-      const float2 o = S0[0];
-      const float gx = divc(fsub(S0[SW].x, S0[-SW].x), c.h2, c.rh2);
-      const float gy = divc(fsub(S0[1].y, S0[-1].y), c.h2, c.rh2);
+      const int o = (r + 1) * SW + cc + 1;
+      const float gx = divc(fsub(sSx[o + SW], sSx[o - SW]), c.h2, c.rh2);
+      const float gy = divc(fsub(sSy[o + 1], sSy[o - 1]), c.h2, c.rh2);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      uso[g] = o.x;
-      uso[NN + g] = o.y;
+      uso[g] = sSx[o];
+      uso[NN + g] = sSy[o];
       rhs[g] = divc(fadd(gx, gy), c.dt, c.rdt);
     });
   }
