@@ -4,7 +4,8 @@ For one (N, scheme, GPU) it times every valid candidate of each stage's launch
 shape with CUDA events (``nsgb_time_stages``: mean device time per launch,
 cold L2 for grids larger than L2) and keeps the fastest per stage:
 
-* stencil tile (width x height cells),
+* stencil launch shape: a tile (width x height cells) of the tiled kernel or
+  a band (width x rows) of the row-streaming kernel,
 * rows per CTA of the row FFTs (forward and inverse),
 * spectrum rows per CTA of the column FFT.
 
@@ -54,9 +55,32 @@ def _key(N: int, scheme: str, device) -> str:
     return f"{torch.cuda.get_device_name(device)}|N={N}|{scheme}"
 
 
-def candidates(N: int) -> dict:
+# Row-streaming stencil: band widths (min(width, N) columns per CTA) and the
+# CTA counts per SM the row bands are sized for.
+ROW_BAND_WIDTHS = [256, 512, 1024, 2048]
+ROW_BAND_WAVES = [1, 2, 3, 4]
+
+
+def row_band_shapes(N: int, sms: int) -> list:
+    """(width, rows) shapes of the row-streaming stencil worth timing for N:
+    each distinct band width, with the row counts that give about 1-4 CTAs
+    per SM (at least 8 rows: a band recomputes 4 rows of its neighbours)."""
+    out = []
+    for W in sorted({min(w, N) for w in ROW_BAND_WIDTHS}):
+        col_bands = N // W
+        for waves in ROW_BAND_WAVES:
+            bands = max(1, -(-waves * sms // col_bands))
+            rows = min(N, max(8, -(-N // bands)))
+            if (W, rows) not in out:
+                out.append((W, rows))
+    return out
+
+
+def candidates(N: int, sms: int = 152) -> dict:
     T = N // min(16, N)
     st = [(w, h) for (w, h) in STENCIL_TILES if w <= N and h <= N]
+    if N >= 256:
+        st += row_band_shapes(N, sms)
     rows = [r for r in ROW_CHOICES if r <= N and (r // 2) * T <= 1024]
     cols = [c for c in COL_CHOICES if c <= N // 2 and c * T <= 512]
     return {"stencil": st, "rows": rows, "cols": cols}
@@ -80,7 +104,7 @@ def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, r
     dt, nu = 1e-4, 1e-3
     cells = N * N
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device) if cells * 28 > (96 << 20) else None
-    cand = candidates(N)
+    cand = candidates(N, torch.cuda.get_device_properties(device).multi_processor_count)
     base = plan.tiles()
     results = {"stencil": {}, "rows": {}, "cols": {}}
     for (w, h) in cand["stencil"]:

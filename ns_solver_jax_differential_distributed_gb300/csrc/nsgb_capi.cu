@@ -74,6 +74,7 @@ struct nsgb_plan {
   float2* tw = nullptr;
   float* k2 = nullptr;
   int tile_w = 64, tile_h = 16, rows_per_cta = 8, cols_per_cta = 2;
+  int adj_w = 64, adj_h = 16;  // tiled-kernel shape of the adjoint stencil
   cudaStream_t graph_stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   std::vector<GraphEntry> graphs;
@@ -85,9 +86,7 @@ namespace {
 // Launch shapes measured best on GB300 by the autotuner (see autotune.py);
 // the autotuner refines them per process.
 void default_tiles(int N, int out[4]) {
-  out[0] = N < 64 ? N : 64;
-  out[1] = N < 16 ? N : (N >= 1024 ? 16 : 8);
-  if (N <= 512 && N >= 64) out[0] = 32;
+  tile_kernel_default(N, out[0], out[1]);
   int rows = N >= 1024 ? 4 : (N >= 256 ? 8 : 16);
   if (rows > N) rows = N;
   out[2] = rows;
@@ -98,8 +97,14 @@ void default_tiles(int N, int out[4]) {
 
 int check_tiles(int N, int tw, int th, int rows, int cols) {
   const int T = N / (N < 16 ? N : 16);
-  if (!stencil_tile_supported(tw, th) || tw > N || th > N)
+  if (stencil_rows_mode(tw)) {
+    if (!stencil_rows_supported(N, tw, th))
+      return fail(NSGB_ERR_INVALID_ARG,
+                  "row-streaming stencil needs a power-of-two band width in [%d, %d] and 1 <= rows <= N "
+                  "(got %dx%d, N=%d)", NSGB_ROWS_MIN_W, NSGB_ROWS_MAX_W, tw, th, N);
+  } else if (!stencil_tile_supported(tw, th) || tw > N || th > N) {
     return fail(NSGB_ERR_INVALID_ARG, "stencil tile %dx%d is not an instantiated shape for N=%d", tw, th, N);
+  }
   if (!is_pow2(rows) || rows < 2 || rows > N || (rows / 2) * T > 1024 ||
       fft_rows_smem_bytes(N, rows) > 200 * 1024)
     return fail(NSGB_ERR_INVALID_ARG, "rows_per_cta %d invalid for N=%d", rows, N);
@@ -236,7 +241,7 @@ struct GradWs {
 
 GradWs carve_grad(const nsgb_plan* plan, int steps, int every, void* ws) {
   const size_t NN = (size_t)plan->N * plan->N;
-  const int nblk = stencil_nblocks(plan->N, plan->tile_w, plan->tile_h);
+  const int nblk = stencil_nblocks(plan->N, plan->adj_w, plan->adj_h);  // adjoint blocks
   GradWs g;
   g.f = carve_rollout(plan, steps, ws);
   Carver cv(ws);
@@ -515,6 +520,7 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   default_tiles(N, t);
   p->tile_w = t[0];
   p->tile_h = t[1];
+  tile_kernel_default(N, p->adj_w, p->adj_h);
   p->rows_per_cta = t[2];
   p->cols_per_cta = t[3];
 
@@ -582,6 +588,10 @@ int nsgb_plan_set_tiles(nsgb_plan* plan, int tw, int th, int rows, int cols) {
   std::lock_guard<std::mutex> lk(plan->mu);
   plan->tile_w = tw;
   plan->tile_h = th;
+  if (!stencil_rows_mode(tw)) {
+    plan->adj_w = tw;
+    plan->adj_h = th;
+  }
   plan->rows_per_cta = rows;
   plan->cols_per_cta = cols;
   return NSGB_OK;
@@ -871,8 +881,9 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   AdjointArgs b;
   b.c = a.c;
   b.scheme = a.scheme;
-  b.tw = a.tw;
-  b.th = a.th;
+  b.tw = plan->adj_w;
+  b.th = plan->adj_h;
+  const int adj_nblk = stencil_nblocks(plan->N, b.tw, b.th);
   b.theta = theta;
   b.theta_len = theta_len;
   b.gpart = g.gpart;
@@ -906,7 +917,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
       }
       lam = lam_out;
     }
-    NSGB_CUDA(launch_greduce(g.gpart, nblk, s1 - s0, g.gacc, st));
+    NSGB_CUDA(launch_greduce(g.gpart, adj_nblk, s1 - s0, g.gacc, st));
   }
   NSGB_CUDA(launch_gfinal(g.gacc, theta_len, dJdtheta, st));
   return NSGB_OK;

@@ -46,12 +46,21 @@ struct StencilArgs {
   int t_from_step = 1;  // t = float(step) * dt (rollout) or t_fixed (single step)
   float t_fixed = 0.f;
   int scheme = 0;
-  int tw = 64, th = 16;  // tile shape (powers of two, <= N)
+  int tw = 64, th = 16;  // tile shape, or row-streaming band (tw >= NSGB_ROWS_MIN_W)
   StepConsts c;
 };
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st);
 int stencil_nblocks(int N, int tw, int th);
 bool stencil_tile_supported(int tw, int th);
+// Launch shapes with tw >= NSGB_ROWS_MIN_W select the row-streaming kernel:
+// bands of min(tw, N) columns (a power of two <= NSGB_ROWS_MAX_W) by th rows.
+constexpr int NSGB_ROWS_MIN_W = 256;
+constexpr int NSGB_ROWS_MAX_W = 2048;
+bool stencil_rows_mode(int tw);
+bool stencil_rows_supported(int N, int tw, int th);
+// Tile of the tiled kernel for N (the adjoint and explicit-force steps use it
+// when the forward stencil streams rows).
+void tile_kernel_default(int N, int& tw, int& th);
 
 // ------------------------------------------------------------- ensembles --
 // Device-resident description of one member of an ensemble advanced by

@@ -221,7 +221,296 @@ __global__ void __launch_bounds__(256) k_stencil_batch(const SolveDev* __restric
   stencil_body<SCHEME, MODE_ROLLOUT, TW, TH>(solves[blockIdx.z].st[variant], step_off);
 }
 
-int stencil_nblocks(int N, int tw, int th) { return (N / tw) * (N / th); }
+// ------------------------------------------------------- row streaming --
+// k_stencil_rows: the same step as k_stencil (MODE_ROLLOUT), computed by
+// threads that march down the grid instead of working on 2-D tiles.
+//
+// A CTA owns the rows [r0, r0 + RH) of a band of W columns (W = N: whole
+// rows, the periodic wrap stays inside the CTA; W < N: one extra group of
+// four halo columns on each side, computed but not stored).  Thread g owns the
+// four consecutive columns of group g (one float4 per field row) and at
+// iteration t
+//   - finishes the projection of row t:  u(t) = u*(t) - dt grad p, from p rows
+//     t-1, t, t+1 in registers and the two p(t) values of the neighbouring
+//     groups,
+//   - forms u*next(t-1) from u(t-2), u(t-1), u(t) (registers) and the edge
+//     values of u(t-1) of the neighbouring groups,
+//   - writes u*next(t-2) and rhs(t-2) = div(u*next)/dt, and adds the row's
+//     objective partial u_x(t-2) f_x.
+// Every per-cell expression is the one k_stencil evaluates, so both kernels
+// give the same bits.  Values from other groups (the first and last column of
+// a group) pass through shared memory, double-buffered by iteration parity,
+// so one barrier per iteration orders them; the rows of iteration t+1 are
+// loaded while iteration t computes.  The i-neighbours never leave registers,
+// which removes most of the shared-memory traffic of the tiled kernel.
+namespace rows {
+
+constexpr int F_P = 0, F_UX = 1, F_UY = 2, F_SY = 3;  // exchanged fields
+
+__host__ __device__ inline int band_width(int N, int tw) { return tw < N ? tw : N; }
+__host__ __device__ inline int groups(int N, int W) { return W == N ? N / 4 : W / 4 + 2; }
+__host__ __device__ inline int threads(int N, int W) { return (groups(N, W) + 31) / 32 * 32; }
+// shared memory: edges [2 slots][4 fields][2 sides][G], forcing rows, 32 sums
+inline size_t smem_bytes(int N, int W, int RH) {
+  return sizeof(float) * ((size_t)16 * groups(N, W) + RH + 2 + 32);
+}
+
+__device__ __forceinline__ float4 ld4(const float* __restrict__ base, size_t off) {
+  return __ldg(reinterpret_cast<const float4*>(base + off));
+}
+__device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
+  *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void unpack(const float4 v, float (&o)[4]) {
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+
+}  // namespace rows
+
+template <int SCHEME>
+__device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step_off) {
+  using namespace rows;
+  const StepConsts& c = a.c;
+  const int N = c.N, M = N - 1;
+  const size_t NN = (size_t)N * N;
+  const int W = band_width(N, a.tw);
+  const bool wrap = (W == N);
+  const int G = groups(N, W);
+  const int RH = a.th;
+  const int r0 = blockIdx.y * RH;
+  const int r1 = min(r0 + RH, N);
+  const int j0 = blockIdx.x * W;
+  const int tid = threadIdx.x;
+  const bool active = tid < G;
+  const int g = active ? tid : G - 1;  // idle lanes shadow the last group
+  const int col = wrap ? 4 * g : ((j0 - 4 + 4 * g) & M);
+  const bool store = active && (wrap || (g >= 1 && g <= G - 2));
+  const int gl = g == 0 ? (wrap ? G - 1 : 0) : g - 1;
+  const int gr = g == G - 1 ? (wrap ? 0 : G - 1) : g + 1;
+
+  extern __shared__ __align__(16) float sm[];
+  float* sE = sm;                  // [slot][field][side][G]
+  float* sF = sm + 16 * G;         // f_x of rows r0-1 .. r1
+  float* sRed = sF + RH + 2;       // per-warp partial sums
+  auto edge = [&](int slot, int f, int side) { return sE + ((slot * 4 + f) * 2 + side) * G; };
+
+  int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
+  const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
+  const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  {
+    const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t_now, c);
+    for (int k = tid; k < r1 - r0 + 2; k += blockDim.x) sF[k] = forcing_fx((r0 - 1 + k) & M, fr, c);
+  }
+
+  const bool has_p = a.p != nullptr;
+  const float* __restrict__ pp = a.p;
+  const float* __restrict__ usx_g = a.us;
+  const float* __restrict__ usy_g = a.us + NN;
+  auto row_off = [&](int r) { return (size_t)(r & M) * N + col; };
+
+  // registers: p rows t-1, t, t+1; u* row t; u rows t-1, t-2; u*next x rows
+  // t-3, t-2 and y row t-2 (entering iteration t)
+  float pm[4] = {0, 0, 0, 0}, pc[4] = {0, 0, 0, 0}, pn[4] = {0, 0, 0, 0};
+  float usx[4], usy[4];
+  float u1x[4] = {0, 0, 0, 0}, u1y[4] = {0, 0, 0, 0}, u2x[4] = {0, 0, 0, 0}, u2y[4] = {0, 0, 0, 0};
+  float sx3[4] = {0, 0, 0, 0}, sx2[4] = {0, 0, 0, 0}, sy2[4] = {0, 0, 0, 0};
+  if (has_p) {
+    unpack(ld4(pp, row_off(r0 - 3)), pm);
+    unpack(ld4(pp, row_off(r0 - 2)), pc);
+    unpack(ld4(pp, row_off(r0 - 1)), pn);
+  }
+  unpack(ld4(usx_g, row_off(r0 - 2)), usx);
+  unpack(ld4(usy_g, row_off(r0 - 2)), usy);
+  if (active) {
+    const int s = (r0 - 3) & 1;
+    edge(s, F_P, 0)[g] = pc[0];
+    edge(s, F_P, 1)[g] = pc[3];
+  }
+  __syncthreads();
+
+  float jacc = 0.0f;
+  float* __restrict__ uso_x = a.us_out;
+  float* __restrict__ uso_y = a.us_out + NN;
+  float* __restrict__ rhs_g = a.rhs;
+#pragma unroll 1
+  for (int t = r0 - 2; t <= r1 + 1; ++t) {
+    const int rs = (t - 1) & 1, ws = t & 1;
+    // rows of the next iteration
+    float4 npn = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (has_p) npn = ld4(pp, row_off(t + 2));
+    const float4 nusx = ld4(usx_g, row_off(t + 1));
+    const float4 nusy = ld4(usy_g, row_off(t + 1));
+
+    // u(t): projection of row t
+    float ux[4], uy[4];
+    if (has_p) {
+      const float P[6] = {edge(rs, F_P, 1)[gl], pc[0], pc[1], pc[2], pc[3], edge(rs, F_P, 0)[gr]};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float px = divc(fsub(pn[k], pm[k]), c.h2, c.rh2);
+        const float py = divc(fsub(P[k + 2], P[k]), c.h2, c.rh2);
+        ux[k] = fsub(usx[k], fmul(c.dt, px));
+        uy[k] = fsub(usy[k], fmul(c.dt, py));
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        ux[k] = usx[k];
+        uy[k] = usy[k];
+      }
+    }
+
+    // u*next(t-1)
+    float sx1[4] = {0, 0, 0, 0}, sy1[4] = {0, 0, 0, 0};
+    if (t >= r0) {
+      const float X[6] = {edge(rs, F_UX, 1)[gl], u1x[0], u1x[1], u1x[2], u1x[3], edge(rs, F_UX, 0)[gr]};
+      const float Y[6] = {edge(rs, F_UY, 1)[gl], u1y[0], u1y[1], u1y[2], u1y[3], edge(rs, F_UY, 0)[gr]};
+      const float fx = sF[t - r0];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float ox = X[k + 1], oy = Y[k + 1];
+        const float lx = u2x[k], rx = ux[k], upx = X[k + 2], dnx = X[k];
+        const float ly = u2y[k], ry = uy[k], upy = Y[k + 2], dny = Y[k];
+        const float lapx = lap5(ox, lx, rx, upx, dnx, c);
+        const float lapy = lap5(oy, ly, ry, upy, dny, c);
+        const float advx = adv5<SCHEME>(ox, lx, rx, upx, dnx, ox, oy, c);
+        const float advy = adv5<SCHEME>(oy, ly, ry, upy, dny, ox, oy, c);
+        sx1[k] = fadd(ox, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
+        sy1[k] = fadd(oy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), 0.0f)));
+      }
+    }
+
+    // u*next(t-2), rhs(t-2), objective partial and state of row t-2
+    if (t >= r0 + 2) {
+      const float Y2[6] = {edge(rs, F_SY, 1)[gl], sy2[0], sy2[1], sy2[2], sy2[3], edge(rs, F_SY, 0)[gr]};
+      float rh[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float gx = divc(fsub(sx1[k], sx3[k]), c.h2, c.rh2);
+        const float gy = divc(fsub(Y2[k + 2], Y2[k]), c.h2, c.rh2);
+        rh[k] = divc(fadd(gx, gy), c.dt, c.rdt);
+      }
+      if (store) {
+        const size_t o = row_off(t - 2);
+        st4(uso_x, o, sx2);
+        st4(uso_y, o, sy2);
+        st4(rhs_g, o, rh);
+        if (a.u_out) {
+          st4(a.u_out, o, u2x);
+          st4(a.u_out + NN, o, u2y);
+        }
+        const float fj = sF[t - r0 - 1];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) jacc += u2x[k] * fj;
+      }
+    }
+
+    // edge values for the next iteration: p(t+1), u(t), u*next_y(t-1)
+    if (active) {
+      edge(ws, F_P, 0)[g] = pn[0];
+      edge(ws, F_P, 1)[g] = pn[3];
+      edge(ws, F_UX, 0)[g] = ux[0];
+      edge(ws, F_UX, 1)[g] = ux[3];
+      edge(ws, F_UY, 0)[g] = uy[0];
+      edge(ws, F_UY, 1)[g] = uy[3];
+      edge(ws, F_SY, 0)[g] = sy1[0];
+      edge(ws, F_SY, 1)[g] = sy1[3];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      pm[k] = pc[k];
+      pc[k] = pn[k];
+      u2x[k] = u1x[k];
+      u2y[k] = u1y[k];
+      u1x[k] = ux[k];
+      u1y[k] = uy[k];
+      sx3[k] = sx2[k];
+      sx2[k] = sx1[k];
+      sy2[k] = sy1[k];
+    }
+    unpack(npn, pn);
+    unpack(nusx, usx);
+    unpack(nusy, usy);
+    __syncthreads();
+  }
+
+  // objective partial of the CTA
+  jacc = warp_sum(jacc);
+  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  if (lane == 0) sRed[warp] = jacc;
+  __syncthreads();
+  if (warp == 0) {
+    float v = lane < nwarps ? sRed[lane] : 0.0f;
+    v = warp_sum(v);
+    if (lane == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
+      const int nblk = gridDim.x * gridDim.y;
+      a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+    }
+  }
+}
+
+template <int SCHEME>
+__global__ void __launch_bounds__(544, 1) k_stencil_rows(const StencilArgs a) {
+  stencil_rows_body<SCHEME>(a, 0);
+}
+
+template <int SCHEME>
+__global__ void __launch_bounds__(544, 1) k_stencil_rows_batch(const SolveDev* __restrict__ solves, int variant,
+                                                              int step_off) {
+  stencil_rows_body<SCHEME>(solves[blockIdx.z].st[variant], step_off);
+}
+
+bool stencil_rows_mode(int tw) { return tw >= NSGB_ROWS_MIN_W; }
+
+bool stencil_rows_supported(int N, int tw, int th) {
+  if (!stencil_rows_mode(tw) || (tw & (tw - 1)) != 0 || tw > NSGB_ROWS_MAX_W) return false;
+  return th >= 1 && th <= N;
+}
+
+// Launch shape of a row-streaming kernel: grid (bands of columns, bands of
+// rows, count), one thread per column group.
+template <class K>
+static cudaError_t rows_config(K kernel, int N, int tw, int th, unsigned count, dim3& grid, dim3& block,
+                               size_t& smem) {
+  const int W = rows::band_width(N, tw);
+  smem = rows::smem_bytes(N, W, th);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  grid = dim3(N / W, (N + th - 1) / th, count);
+  block = dim3(rows::threads(N, W));
+  return cudaSuccess;
+}
+
+template <int SCHEME>
+static cudaError_t launch_stencil_rows(const StencilArgs& a, cudaStream_t st) {
+  dim3 grid, block;
+  size_t smem;
+  cudaError_t e = rows_config(k_stencil_rows<SCHEME>, a.c.N, a.tw, a.th, 1, grid, block, smem);
+  if (e != cudaSuccess) return e;
+  k_stencil_rows<SCHEME><<<grid, block, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int SCHEME>
+static cudaError_t launch_stencil_rows_batch(const SolveDev* solves, int count, int variant, int step_off, int N,
+                                             int tw, int th, cudaStream_t st) {
+  dim3 grid, block;
+  size_t smem;
+  cudaError_t e = rows_config(k_stencil_rows_batch<SCHEME>, N, tw, th, (unsigned)count, grid, block, smem);
+  if (e != cudaSuccess) return e;
+  k_stencil_rows_batch<SCHEME><<<grid, block, smem, st>>>(solves, variant, step_off);
+  return cudaGetLastError();
+}
+
+int stencil_nblocks(int N, int tw, int th) {
+  if (stencil_rows_mode(tw)) return (N / rows::band_width(N, tw)) * ((N + th - 1) / th);
+  return (N / tw) * (N / th);
+}
 
 bool stencil_tile_supported(int tw, int th) {
 #define NSGB_TILE_OK(W, H) if (tw == W && th == H) return true;
@@ -275,6 +564,10 @@ static cudaError_t launch_stencil_batch_s(const SolveDev* solves, int count, int
 
 cudaError_t launch_stencil_batch(const SolveDev* solves, int count, int variant, int step_off, int scheme, int N,
                                  int tw, int th, cudaStream_t st) {
+  if (stencil_rows_mode(tw))
+    return scheme == NSGB_SCHEME_CENTRAL
+               ? launch_stencil_rows_batch<NSGB_SCHEME_CENTRAL>(solves, count, variant, step_off, N, tw, th, st)
+               : launch_stencil_rows_batch<NSGB_SCHEME_UPWIND>(solves, count, variant, step_off, N, tw, th, st);
   return scheme == NSGB_SCHEME_CENTRAL
              ? launch_stencil_batch_s<NSGB_SCHEME_CENTRAL>(solves, count, variant, step_off, N, tw, th, st)
              : launch_stencil_batch_s<NSGB_SCHEME_UPWIND>(solves, count, variant, step_off, N, tw, th, st);
@@ -289,7 +582,21 @@ static cudaError_t launch_stencil_s(const StencilArgs& a, cudaStream_t st) {
   return cudaErrorInvalidValue;
 }
 
+void tile_kernel_default(int N, int& tw, int& th) {
+  tw = N < 64 ? N : (N <= 512 ? 32 : 64);
+  th = N < 16 ? N : (N >= 1024 ? 16 : 8);
+}
+
 cudaError_t launch_stencil(const StencilArgs& a, int mode, cudaStream_t st) {
+  if (stencil_rows_mode(a.tw)) {
+    if (mode == MODE_ROLLOUT)
+      return a.scheme == NSGB_SCHEME_CENTRAL ? launch_stencil_rows<NSGB_SCHEME_CENTRAL>(a, st)
+                                             : launch_stencil_rows<NSGB_SCHEME_UPWIND>(a, st);
+    // explicit force fields: the tiled kernel
+    StencilArgs b = a;
+    tile_kernel_default(a.c.N, b.tw, b.th);
+    return launch_stencil(b, mode, st);
+  }
   if (a.scheme == NSGB_SCHEME_CENTRAL) {
     return mode == MODE_ROLLOUT ? launch_stencil_s<NSGB_SCHEME_CENTRAL, MODE_ROLLOUT>(a, st)
                                 : launch_stencil_s<NSGB_SCHEME_CENTRAL, MODE_FIELD>(a, st);
