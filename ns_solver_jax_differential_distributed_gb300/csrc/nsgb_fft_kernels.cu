@@ -50,9 +50,10 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   const float* ra = rhs + (size_t)(i0 + 2 * pp) * N;
   const float* rb = ra + N;
 
+  // Row data is read once: evict-first loads keep the twiddle tables in L1.
   float2 a[E];
 #pragma unroll
-  for (int s = 0; s < E; ++s) a[s] = make_float2(__ldg(ra + j + s * T), __ldg(rb + j + s * T));
+  for (int s = 0; s < E; ++s) a[s] = make_float2(__ldcs(ra + j + s * T), __ldcs(rb + j + s * T));
   fft::block_fft<N, false>(a, sb, j, tw);
   __syncthreads();
 #pragma unroll
@@ -100,7 +101,7 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
 
   float2 a[E];
 #pragma unroll
-  for (int s = 0; s < E; ++s) a[s] = row[j + s * T];
+  for (int s = 0; s < E; ++s) a[s] = __ldcs(row + j + s * T);
   fft::block_fft<N, false>(a, sb, j, tw);
 
   const float k2y = __ldg(k2 + ky);
@@ -132,13 +133,24 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   const int nth = T * P;
 
   // Stage the RB half-spectrum rows: pair buffer (r>>1) holds X_a[k] at k
-  // and X_b[k] at H + 1 + k, k = 0..H.
-  for (int e = tid; e < RB * (H + 1); e += nth) {
+  // and X_b[k] at H + 1 + k, k = 0..H.  The strided loads are issued in
+  // batches of 8 before their shared-memory stores, so their latencies overlap.
+  const int tot = RB * (H + 1);
+  auto stage = [&](int e, float2 v) {
     const int r = e & (RB - 1);
     const int k = e / RB;
-    const float2 v = __ldg(spec + (size_t)k * N + i0 + r);
     smem2[(r >> 1) * pair_stride<N>() + pad((r & 1) * (H + 1) + k)] = v;
+  };
+  auto src = [&](int e) { return spec + (size_t)(e / RB) * N + i0 + (e & (RB - 1)); };
+  int e = tid;
+  for (; e + 7 * nth < tot; e += 8 * nth) {
+    float2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldcs(src(e + u * nth));
+#pragma unroll
+    for (int u = 0; u < 8; ++u) stage(e + u * nth, v[u]);
   }
+  for (; e < tot; e += nth) stage(e, __ldcs(src(e)));
   __syncthreads();
 
   float2* sb = smem2 + pp * pair_stride<N>();

@@ -270,8 +270,10 @@ __device__ __forceinline__ void unpack(const float4 v, float (&o)[4]) {
 
 }  // namespace rows
 
-template <int SCHEME>
+// PF: rows loaded ahead (1: the rows of iteration t+1 are loaded at t).
+template <int SCHEME, int PF>
 __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step_off) {
+  static_assert(PF >= 1 && PF <= 3, "prefetch depth");
   using namespace rows;
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
@@ -324,6 +326,14 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   }
   unpack(ld4(usx_g, row_off(r0 - 2)), usx);
   unpack(ld4(usy_g, row_off(r0 - 2)), usy);
+  // queued rows entering iteration t: p(t+2+k), u*(t+1+k), k < PF-1
+  float4 qp[PF], qx[PF], qy[PF];
+#pragma unroll
+  for (int k = 0; k < PF - 1; ++k) {
+    qp[k] = has_p ? ld4(pp, row_off(r0 + k)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    qx[k] = ld4(usx_g, row_off(r0 - 1 + k));
+    qy[k] = ld4(usy_g, row_off(r0 - 1 + k));
+  }
   if (active) {
     const int s = (r0 - 3) & 1;
     edge(s, F_P, 0)[g] = pc[0];
@@ -338,11 +348,10 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
 #pragma unroll 1
   for (int t = r0 - 2; t <= r1 + 1; ++t) {
     const int rs = (t - 1) & 1, ws = t & 1;
-    // rows of the next iteration
-    float4 npn = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (has_p) npn = ld4(pp, row_off(t + 2));
-    const float4 nusx = ld4(usx_g, row_off(t + 1));
-    const float4 nusy = ld4(usy_g, row_off(t + 1));
+    // rows of iteration t + PF
+    qp[PF - 1] = has_p ? ld4(pp, row_off(t + 1 + PF)) : make_float4(0.f, 0.f, 0.f, 0.f);
+    qx[PF - 1] = ld4(usx_g, row_off(t + PF));
+    qy[PF - 1] = ld4(usy_g, row_off(t + PF));
 
     // u(t): projection of row t
     float ux[4], uy[4];
@@ -431,9 +440,15 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       sx2[k] = sx1[k];
       sy2[k] = sy1[k];
     }
-    unpack(npn, pn);
-    unpack(nusx, usx);
-    unpack(nusy, usy);
+    unpack(qp[0], pn);
+    unpack(qx[0], usx);
+    unpack(qy[0], usy);
+#pragma unroll
+    for (int k = 0; k < PF - 1; ++k) {
+      qp[k] = qp[k + 1];
+      qx[k] = qx[k + 1];
+      qy[k] = qy[k + 1];
+    }
     __syncthreads();
   }
 
@@ -452,15 +467,17 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   }
 }
 
+constexpr int kRowsPrefetch = 1;
+
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows(const StencilArgs a) {
-  stencil_rows_body<SCHEME>(a, 0);
+  stencil_rows_body<SCHEME, kRowsPrefetch>(a, 0);
 }
 
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows_batch(const SolveDev* __restrict__ solves, int variant,
                                                               int step_off) {
-  stencil_rows_body<SCHEME>(solves[blockIdx.z].st[variant], step_off);
+  stencil_rows_body<SCHEME, kRowsPrefetch>(solves[blockIdx.z].st[variant], step_off);
 }
 
 bool stencil_rows_mode(int tw) { return tw >= NSGB_ROWS_MIN_W; }
