@@ -165,6 +165,11 @@ StepConsts make_consts(const nsgb_plan* plan, const nsgb_phys* ph) {
   c.rh2 = recip_rn(c.h2);
   c.rdx2 = recip_rn(c.dx2);
   c.rdt = recip_rn(c.dt);
+  c.cP = (float)((double)c.dt / c.h2);
+  c.cD = (float)(1.0 / ((double)c.h2 * c.dt));
+  c.cAc = (float)((double)c.dt / c.h2);
+  c.cAu = (float)((double)c.dt / c.h1);
+  c.dtdx2 = (float)((double)c.dt / c.dx2);
   return c;
 }
 

@@ -2,8 +2,9 @@
 //
 // Arithmetic that mirrors the reference's elementwise expressions is written
 // with explicit round-to-nearest intrinsics (__fadd_rn, __fmul_rn, ...) so the
-// compiler cannot contract it into FMAs: the stencils then round exactly like
-// the reference's float32 array expressions (NS_solver.py:243-265, 687-697).
+// compiler cannot contract it into FMAs: the single-operator stencils then
+// round exactly like the reference's float32 array expressions
+// (NS_solver.py:243-265).  The fused step uses the folded forms below.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -55,7 +56,52 @@ struct StepConsts {
   float jscale; // dt * dx**2 in double, applied at the reduction
   // correctly rounded reciprocals of the divisors (for divc)
   float rh1, rh2, rdx2, rdt;
+  // coefficients of the fused step (each rounded once from double):
+  float cP;     // dt / h2          projection     u = u* - cP (p(i+1) - p(i-1))
+  float cD;     // 1 / (h2 dt)      rhs = cD (dx-difference + dy-difference)
+  float cAc;    // dt / h2          central advection
+  float cAu;    // dt / h1          upwind advection
+  float dtdx2;  // dt / dx^2        (times nu: the diffusion coefficient)
 };
+
+// ------------------------------------------------------- fused-step cells --
+// The per-cell arithmetic of the fused Chorin step (NS_solver.py:685-697):
+// the reference's expressions with their constant divisions folded into the
+// coefficients above and explicit FMAs, so a cell costs about half the
+// instructions of the operator-by-operator form.  Every op is an explicitly
+// rounded intrinsic, so each kernel that uses these helpers produces the same
+// bits; against the reference's own rounding order the results differ by a
+// few ulps per step.
+
+// u = u* - dt dp/dh from the two neighbours of the projected direction.
+__device__ __forceinline__ float fused_proj(float us, float p_plus, float p_minus, float cP) {
+  return __fmaf_rn(-cP, __fsub_rn(p_plus, p_minus), us);
+}
+
+// u*next = u + dt (nu lap u + adv(u) + f) for one velocity component:
+// o centre, l/r its i-1/i+1 neighbours, dn/up its j-1/j+1 neighbours, (ux, uy)
+// the velocity at the cell, cL = dt nu / dx^2, cF = dt f.
+template <int SCHEME>
+__device__ __forceinline__ float fused_ustar(float o, float l, float r, float up, float dn, float ux, float uy,
+                                             float cL, float cF, const StepConsts& c) {
+  const float lap = __fmaf_rn(-4.0f, o, __fadd_rn(__fadd_rn(l, r), __fadd_rn(up, dn)));
+  float a, cA;
+  if (SCHEME == NSGB_SCHEME_CENTRAL) {
+    a = __fmaf_rn(ux, __fsub_rn(r, l), __fmul_rn(uy, __fsub_rn(up, dn)));
+    cA = c.cAc;
+  } else {
+    const float gx = ux >= 0.0f ? __fsub_rn(o, l) : __fsub_rn(r, o);
+    const float gy = uy >= 0.0f ? __fsub_rn(o, dn) : __fsub_rn(up, o);
+    a = __fmaf_rn(ux, gx, __fmul_rn(uy, gy));
+    cA = c.cAu;
+  }
+  return __fadd_rn(o, __fmaf_rn(-cA, a, __fmaf_rn(cL, lap, cF)));
+}
+
+// rhs = div(u*)/dt from the i-neighbours of u*_x and the j-neighbours of u*_y.
+__device__ __forceinline__ float fused_rhs(float xp, float xm, float yp, float ym, float cD) {
+  return __fmul_rn(__fadd_rn(__fsub_rn(xp, xm), __fsub_rn(yp, ym)), cD);
+}
 
 // Gaussian forcing fx at row i for time t (NS_solver.py:621-627):
 //   mu = mu0 + sin(2 pi A t); sig = sigma0 + cos(2 pi B t)^2;

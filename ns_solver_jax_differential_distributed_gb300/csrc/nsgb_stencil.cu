@@ -11,35 +11,14 @@
 //      1-cell halo (NS_solver.py:685-689, 249-265, 474-477),
 //   4. writes u*^{n+1} and rhs = div(u*^{n+1}) / dt for the tile
 //      (NS_solver.py:692-693, 206-210).
-// The elementwise arithmetic keeps the reference's operation order with
-// explicitly rounded intrinsics (no FMA contraction), so it rounds exactly
-// like the reference's float32 array expressions.
+// The fused step evaluates each cell with the folded-coefficient FMA forms of
+// nsgb_common.cuh (fused_proj / fused_ustar / fused_rhs); the single-operator
+// kernels at the end of the file keep the reference's operation order with
+// explicitly rounded intrinsics, so they round exactly like the reference's
+// float32 array expressions.
 #include "nsgb_internal.h"
 
 namespace nsgb {
-
-// 5-point Laplacian from the centre value and its four neighbours
-// (left/right = i -+ 1, down/up = j -+ 1; NS_solver.py:249-255).
-__device__ __forceinline__ float lap5(float f, float left, float right, float up, float down,
-                                      const StepConsts& c) {
-  return divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f)), c.dx2, c.rdx2);
-}
-
-// -(u . grad) f from the same five values (NS_solver.py:474-477 central,
-// :257-265 upwind).
-template <int SCHEME>
-__device__ __forceinline__ float adv5(float f, float left, float right, float up, float down, float ux,
-                                      float uy, const StepConsts& c) {
-  if (SCHEME == NSGB_SCHEME_CENTRAL) {
-    const float gx = divc(fsub(right, left), c.h2, c.rh2);
-    const float gy = divc(fsub(up, down), c.h2, c.rh2);
-    return -fadd(fmul(ux, gx), fmul(uy, gy));
-  } else {
-    const float dfx = divc(ux >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1, c.rh1);
-    const float dfy = divc(uy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1, c.rh1);
-    return -fadd(fmul(ux, dfx), fmul(uy, dfy));
-  }
-}
 
 // Shared-memory layout of one TW x TH tile (TW a multiple of 4, TH even).
 // Tiles are fetched from HBM as aligned float4 groups covering columns
@@ -87,6 +66,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     if (a.t_from_step) t = fmul((float)step, c.dt);
   }
   const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float cL = fmul(c.dtdx2, nu);
 
   // Tile loads: aligned float4 groups (a group never straddles the periodic
   // wrap because N and the group start are multiples of 4).
@@ -119,11 +99,9 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     forflat<UH, TW + 4>(tid, [&](int r, int cc) {
       const int col = cc + 2;
       const float* P0 = sP + (r + 1) * W4 + col;  // p at (i0-2+r, j0-2+cc)
-      const float px = divc(fsub(P0[W4], P0[-W4]), c.h2, c.rh2);
-      const float py = divc(fsub(P0[1], P0[-1]), c.h2, c.rh2);
       const int o = r * W4 + col;
-      sUx[o] = fsub(sUx[o], fmul(c.dt, px));
-      sUy[o] = fsub(sUy[o], fmul(c.dt, py));
+      sUx[o] = fused_proj(sUx[o], P0[W4], P0[-W4], c.cP);
+      sUy[o] = fused_proj(sUy[o], P0[1], P0[-1], c.cP);
     });
     __syncthreads();
   }
@@ -158,10 +136,6 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
       const float ox = x[k + 1], oy = y[k + 1];
       const float lx = x[k], rx = x[k + 2], ux_ = sUx[ok + 1], dx_ = sUx[ok - 1];
       const float ly = y[k], ry = y[k + 2], uy_ = sUy[ok + 1], dy_ = sUy[ok - 1];
-      const float lapx = lap5(ox, lx, rx, ux_, dx_, c);
-      const float lapy = lap5(oy, ly, ry, uy_, dy_, c);
-      const float advx = adv5<SCHEME>(ox, lx, rx, ux_, dx_, ox, oy, c);
-      const float advy = adv5<SCHEME>(oy, ly, ry, uy_, dy_, ox, oy, c);
       float fx, fy;
       if (MODE == MODE_ROLLOUT) {
         fx = sF[r + k];
@@ -172,8 +146,8 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
         fy = __ldg(a.f + NN + g);
       }
       const int so = (r + k) * SW + cc;
-      sSx[so] = fadd(ox, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
-      sSy[so] = fadd(oy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), fy)));
+      sSx[so] = fused_ustar<SCHEME>(ox, lx, rx, ux_, dx_, ox, oy, cL, fmul(c.dt, fx), c);
+      sSy[so] = fused_ustar<SCHEME>(oy, ly, ry, uy_, dy_, ox, oy, cL, fmul(c.dt, fy), c);
     }
   });
   __syncthreads();
@@ -184,12 +158,10 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     float* __restrict__ rhs = a.rhs;
     forflat<TH, TW>(tid, [&](int r, int cc) {
       const int o = (r + 1) * SW + cc + 1;
-      const float gx = divc(fsub(sSx[o + SW], sSx[o - SW]), c.h2, c.rh2);
-      const float gy = divc(fsub(sSy[o + 1], sSy[o - 1]), c.h2, c.rh2);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
       uso[g] = sSx[o];
       uso[NN + g] = sSy[o];
-      rhs[g] = divc(fadd(gx, gy), c.dt, c.rdt);
+      rhs[g] = fused_rhs(sSx[o + SW], sSx[o - SW], sSy[o + 1], sSy[o - 1], c.cD);
     });
   }
 
@@ -302,6 +274,7 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
   const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
   const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float cL = fmul(c.dtdx2, nu);
   {
     const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t_now, c);
     for (int k = tid; k < r1 - r0 + 2; k += blockDim.x) sF[k] = forcing_fx((r0 - 1 + k) & M, fr, c);
@@ -359,10 +332,8 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       const float P[6] = {edge(rs, F_P, 1)[gl], pc[0], pc[1], pc[2], pc[3], edge(rs, F_P, 0)[gr]};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        const float px = divc(fsub(pn[k], pm[k]), c.h2, c.rh2);
-        const float py = divc(fsub(P[k + 2], P[k]), c.h2, c.rh2);
-        ux[k] = fsub(usx[k], fmul(c.dt, px));
-        uy[k] = fsub(usy[k], fmul(c.dt, py));
+        ux[k] = fused_proj(usx[k], pn[k], pm[k], c.cP);
+        uy[k] = fused_proj(usy[k], P[k + 2], P[k], c.cP);
       }
     } else {
 #pragma unroll
@@ -377,18 +348,12 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
     if (t >= r0) {
       const float X[6] = {edge(rs, F_UX, 1)[gl], u1x[0], u1x[1], u1x[2], u1x[3], edge(rs, F_UX, 0)[gr]};
       const float Y[6] = {edge(rs, F_UY, 1)[gl], u1y[0], u1y[1], u1y[2], u1y[3], edge(rs, F_UY, 0)[gr]};
-      const float fx = sF[t - r0];
+      const float cFx = fmul(c.dt, sF[t - r0]), cFy = fmul(c.dt, 0.0f);
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const float ox = X[k + 1], oy = Y[k + 1];
-        const float lx = u2x[k], rx = ux[k], upx = X[k + 2], dnx = X[k];
-        const float ly = u2y[k], ry = uy[k], upy = Y[k + 2], dny = Y[k];
-        const float lapx = lap5(ox, lx, rx, upx, dnx, c);
-        const float lapy = lap5(oy, ly, ry, upy, dny, c);
-        const float advx = adv5<SCHEME>(ox, lx, rx, upx, dnx, ox, oy, c);
-        const float advy = adv5<SCHEME>(oy, ly, ry, upy, dny, ox, oy, c);
-        sx1[k] = fadd(ox, fmul(c.dt, fadd(fadd(fmul(nu, lapx), advx), fx)));
-        sy1[k] = fadd(oy, fmul(c.dt, fadd(fadd(fmul(nu, lapy), advy), 0.0f)));
+        sx1[k] = fused_ustar<SCHEME>(ox, u2x[k], ux[k], X[k + 2], X[k], ox, oy, cL, cFx, c);
+        sy1[k] = fused_ustar<SCHEME>(oy, u2y[k], uy[k], Y[k + 2], Y[k], ox, oy, cL, cFy, c);
       }
     }
 
@@ -397,11 +362,7 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       const float Y2[6] = {edge(rs, F_SY, 1)[gl], sy2[0], sy2[1], sy2[2], sy2[3], edge(rs, F_SY, 0)[gr]};
       float rh[4];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float gx = divc(fsub(sx1[k], sx3[k]), c.h2, c.rh2);
-        const float gy = divc(fsub(Y2[k + 2], Y2[k]), c.h2, c.rh2);
-        rh[k] = divc(fadd(gx, gy), c.dt, c.rdt);
-      }
+      for (int k = 0; k < 4; ++k) rh[k] = fused_rhs(sx1[k], sx3[k], Y2[k + 2], Y2[k], c.cD);
       if (store) {
         const size_t o = row_off(t - 2);
         st4(uso_x, o, sx2);
@@ -630,12 +591,10 @@ __global__ void k_project(const float* __restrict__ us, const float* __restrict_
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
-  const float px = divc(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
-                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2);
-  const float py = divc(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
-                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2);
-  u[g] = fsub(__ldg(us + g), fmul(c.dt, px));
-  u[NN + g] = fsub(__ldg(us + NN + g), fmul(c.dt, py));
+  u[g] = fused_proj(__ldg(us + g), __ldg(p + (size_t)((i + 1) & M) * N + j),
+                    __ldg(p + (size_t)((i - 1) & M) * N + j), c.cP);
+  u[NN + g] = fused_proj(__ldg(us + NN + g), __ldg(p + (size_t)i * N + ((j + 1) & M)),
+                         __ldg(p + (size_t)i * N + ((j - 1) & M)), c.cP);
 }
 
 cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
@@ -655,12 +614,10 @@ __global__ void k_project_batch(const SolveDev* __restrict__ solves, int variant
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
   const float* p = a.p;
-  const float px = divc(fsub(__ldg(p + (size_t)((i + 1) & M) * N + j),
-                             __ldg(p + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2);
-  const float py = divc(fsub(__ldg(p + (size_t)i * N + ((j + 1) & M)),
-                             __ldg(p + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2);
-  d.u_final[g] = fsub(__ldg(a.us + g), fmul(c.dt, px));
-  d.u_final[NN + g] = fsub(__ldg(a.us + NN + g), fmul(c.dt, py));
+  d.u_final[g] = fused_proj(__ldg(a.us + g), __ldg(p + (size_t)((i + 1) & M) * N + j),
+                            __ldg(p + (size_t)((i - 1) & M) * N + j), c.cP);
+  d.u_final[NN + g] = fused_proj(__ldg(a.us + NN + g), __ldg(p + (size_t)i * N + ((j + 1) & M)),
+                                 __ldg(p + (size_t)i * N + ((j - 1) & M)), c.cP);
 }
 
 // Projection of the final state of every solve: `variant` names the argument
