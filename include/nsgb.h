@@ -74,11 +74,21 @@ const char* nsgb_last_error(void);
 int nsgb_plan_create(int N, double L, nsgb_plan** plan);
 int nsgb_plan_destroy(nsgb_plan* plan);
 
-/* Launch shapes used by the plan's kernels: stencil tile (tw x th cells),
- * rows per CTA of the row FFTs, k-rows per CTA of the column FFT.  All
- * powers of two; 0 keeps the current value.  Chosen by the autotuner. */
+/* No counterpart in the reference (launch tuning).  Launch shapes used by
+ * the plan's kernels: the stencil shape -- a tile of tw x th cells (tw <= 128)
+ * of the tiled kernel, or for tw >= 256 a band of min(tw, N) columns by th
+ * rows of the row-streaming kernel -- then rows per CTA of the row FFTs and
+ * k-rows per CTA of the column FFT.  0 keeps the current value.  Chosen by
+ * the autotuner; results do not depend on them. */
 int nsgb_plan_set_tiles(nsgb_plan* plan, int tw, int th, int rows_per_cta, int cols_per_cta);
 int nsgb_plan_get_tiles(const nsgb_plan* plan, int out[4]);
+
+/* No counterpart in the reference (launch tuning).  Stockham radix (16 or 8)
+ * of the row passes and of the column pass of the FFT-Poisson solve; 0 keeps
+ * the current value.  Radix 8 carries a transform on twice as many threads
+ * with half the registers each.  Results agree to FFT rounding. */
+int nsgb_plan_set_fft_radix(nsgb_plan* plan, int radix_rows, int radix_cols);
+int nsgb_plan_get_fft_radix(const nsgb_plan* plan, int out[2]);
 
 /* Bytes of workspace for nsgb_poisson / nsgb_projector_step / nsgb_step. */
 size_t nsgb_poisson_workspace_bytes(const nsgb_plan* plan);

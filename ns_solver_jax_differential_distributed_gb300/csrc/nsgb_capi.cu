@@ -61,7 +61,7 @@ struct GraphEntry {
   int chunk = 0;
   StepConsts c{};
   int scheme = 0;
-  int tiles[4] = {0, 0, 0, 0};
+  int tiles[6] = {0, 0, 0, 0, 0, 0};
   cudaGraphExec_t exec = nullptr;
 };
 
@@ -75,6 +75,7 @@ struct nsgb_plan {
   float* k2 = nullptr;
   int tile_w = 64, tile_h = 16, rows_per_cta = 8, cols_per_cta = 2;
   int adj_w = 64, adj_h = 16;  // tiled-kernel shape of the adjoint stencil
+  int radix_rows = 16, radix_cols = 16;  // Stockham radix of the FFT passes
   cudaStream_t graph_stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   std::vector<GraphEntry> graphs;
@@ -95,8 +96,9 @@ void default_tiles(int N, int out[4]) {
   out[3] = kb;
 }
 
-int check_tiles(int N, int tw, int th, int rows, int cols) {
-  const int T = N / (N < 16 ? N : 16);
+int check_tiles(int N, int tw, int th, int rows, int cols, int radix_rows, int radix_cols) {
+  const int Tr = N / (N < radix_rows ? N : radix_rows);
+  const int Tc = N / (N < radix_cols ? N : radix_cols);
   if (stencil_rows_mode(tw)) {
     if (!stencil_rows_supported(N, tw, th))
       return fail(NSGB_ERR_INVALID_ARG,
@@ -105,11 +107,11 @@ int check_tiles(int N, int tw, int th, int rows, int cols) {
   } else if (!stencil_tile_supported(tw, th) || tw > N || th > N) {
     return fail(NSGB_ERR_INVALID_ARG, "stencil tile %dx%d is not an instantiated shape for N=%d", tw, th, N);
   }
-  if (!is_pow2(rows) || rows < 2 || rows > N || (rows / 2) * T > 1024 ||
+  if (!is_pow2(rows) || rows < 2 || rows > N || (rows / 2) * Tr > 1024 ||
       fft_rows_smem_bytes(N, rows) > 200 * 1024)
-    return fail(NSGB_ERR_INVALID_ARG, "rows_per_cta %d invalid for N=%d", rows, N);
-  if (!is_pow2(cols) || cols > N / 2 || cols * T > 512 || fft_cols_smem_bytes(N, cols) > 200 * 1024)
-    return fail(NSGB_ERR_INVALID_ARG, "cols_per_cta %d invalid for N=%d", cols, N);
+    return fail(NSGB_ERR_INVALID_ARG, "rows_per_cta %d invalid for N=%d (radix %d)", rows, N, radix_rows);
+  if (!is_pow2(cols) || cols > N / 2 || cols * Tc > 512 || fft_cols_smem_bytes(N, cols) > 200 * 1024)
+    return fail(NSGB_ERR_INVALID_ARG, "cols_per_cta %d invalid for N=%d (radix %d)", cols, N, radix_cols);
   return NSGB_OK;
 }
 
@@ -184,6 +186,8 @@ FftLaunch fft_launch(const nsgb_plan* plan, const float* rhs, void* spec, float*
   L.scale = (float)(1.0 / (2.0 * (double)plan->N * (double)plan->N));
   L.rows_per_cta = plan->rows_per_cta;
   L.cols_per_cta = plan->cols_per_cta;
+  L.radix_rows = plan->radix_rows;
+  L.radix_cols = plan->radix_cols;
   return L;
 }
 
@@ -529,19 +533,11 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   p->rows_per_cta = t[2];
   p->cols_per_cta = t[3];
 
-  // Per-pass twiddle tables of the Stockham FFT (layout in nsgb_fft.cuh):
-  // the pass with stride ns and radix rp stores W_{ns*rp}^{bm*r} at
-  // off + r*ns + bm, computed in double and rounded to float.
-  const int ntw = nsgb::fft::tw_entries(N);
-  std::vector<float2> tw(ntw, make_float2(1.f, 0.f));
-  for (int ns = 16, off = 0; ns < N; off += (N / ns >= 16 ? 16 : N / ns) * ns, ns *= 16) {
-    const int rp = N / ns >= 16 ? 16 : N / ns;
-    for (int r = 1; r < rp; ++r)
-      for (int bm = 0; bm < ns; ++bm) {
-        const double ang = -2.0 * M_PI * (double)bm * r / ((double)ns * rp);
-        tw[off + r * ns + bm] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-      }
-  }
+  // Per-pass twiddle tables of the Stockham FFT, radix 16 then radix 8
+  // (layout in nsgb_fft.cuh).
+  const int ntw = nsgb::fft::tw_total(N);
+  std::vector<float2> tw(ntw);
+  nsgb::fft::host_twiddles(N, tw.data());
   // k = 2 pi fftfreq(N, dx) in float32 as NS_solver.py:518-519 evaluates it:
   // (m / float32(dx*N)) * 2 * float32(pi), then squared in float32.
   std::vector<float> k2(N);
@@ -589,7 +585,7 @@ int nsgb_plan_set_tiles(nsgb_plan* plan, int tw, int th, int rows, int cols) {
   th = th ? th : plan->tile_h;
   rows = rows ? rows : plan->rows_per_cta;
   cols = cols ? cols : plan->cols_per_cta;
-  if (int r = check_tiles(plan->N, tw, th, rows, cols)) return r;
+  if (int r = check_tiles(plan->N, tw, th, rows, cols, plan->radix_rows, plan->radix_cols)) return r;
   std::lock_guard<std::mutex> lk(plan->mu);
   plan->tile_w = tw;
   plan->tile_h = th;
@@ -599,6 +595,29 @@ int nsgb_plan_set_tiles(nsgb_plan* plan, int tw, int th, int rows, int cols) {
   }
   plan->rows_per_cta = rows;
   plan->cols_per_cta = cols;
+  return NSGB_OK;
+}
+
+int nsgb_plan_set_fft_radix(nsgb_plan* plan, int radix_rows, int radix_cols) {
+  if (int r = check_plan(plan)) return r;
+  radix_rows = radix_rows ? radix_rows : plan->radix_rows;
+  radix_cols = radix_cols ? radix_cols : plan->radix_cols;
+  if ((radix_rows != 8 && radix_rows != 16) || (radix_cols != 8 && radix_cols != 16))
+    return fail(NSGB_ERR_INVALID_ARG, "FFT radix must be 8 or 16 (got %d, %d)", radix_rows, radix_cols);
+  if (int r = check_tiles(plan->N, plan->tile_w, plan->tile_h, plan->rows_per_cta, plan->cols_per_cta,
+                          radix_rows, radix_cols))
+    return r;
+  std::lock_guard<std::mutex> lk(plan->mu);
+  plan->radix_rows = radix_rows;
+  plan->radix_cols = radix_cols;
+  return NSGB_OK;
+}
+
+int nsgb_plan_get_fft_radix(const nsgb_plan* plan, int out[2]) {
+  if (int r = check_plan(plan)) return r;
+  if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
+  out[0] = plan->radix_rows;
+  out[1] = plan->radix_cols;
   return NSGB_OK;
 }
 
@@ -769,7 +788,8 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
       if (g.ws == workspace && g.steps == steps && g.theta == theta && g.theta_len == theta_len && g.chunk == K &&
           g.scheme == a.scheme && std::memcmp(&g.c, &a.c, sizeof(StepConsts)) == 0 &&
           g.tiles[0] == plan->tile_w && g.tiles[1] == plan->tile_h && g.tiles[2] == plan->rows_per_cta &&
-          g.tiles[3] == plan->cols_per_cta) {
+          g.tiles[3] == plan->cols_per_cta && g.tiles[4] == plan->radix_rows &&
+          g.tiles[5] == plan->radix_cols) {
         ge = &g;
         break;
       }
@@ -809,6 +829,8 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
       g.tiles[1] = plan->tile_h;
       g.tiles[2] = plan->rows_per_cta;
       g.tiles[3] = plan->cols_per_cta;
+      g.tiles[4] = plan->radix_rows;
+      g.tiles[5] = plan->radix_cols;
       cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
       cudaGraphDestroy(graph);
       if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");

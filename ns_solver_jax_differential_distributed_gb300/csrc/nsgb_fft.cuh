@@ -1,20 +1,25 @@
 // Block-level FFT building blocks for power-of-two lengths 16..4096.
 //
-// A transform of length N is carried by T = N/E threads, each holding E =
-// min(16, N) complex values in registers.  Thread j holds elements j + s*T
+// A transform of length N is carried by T = N/E threads, each holding E
+// complex values in registers (E = 16 or 8, at most N).  Thread j holds elements j + s*T
 // (s = 0..E-1) on entry and X[j + s*T] on exit, so the first pass reads and
 // the last pass writes "natural" strided positions; rows stored contiguously
 // in global memory are therefore loaded and stored fully coalesced.
 //
-// The transform is the radix-16 Stockham autosort algorithm (a final pass of
-// radix 2/4/8 when log2(N) is not a multiple of 4).  Between passes the values
+// The transform is the radix-E Stockham autosort algorithm (a final pass of
+// smaller radix when log2(N) is not a multiple of log2(E)).  Radix 8 needs
+// half the registers per thread of radix 16 for the same arithmetic, so twice
+// as many threads (and warps) carry a transform.  Between passes the values
 // are exchanged through shared memory as float2, padded by one element every
 // 16 (index i -> i + i/16), which keeps the 64-bit pass writes and reads
 // bank-conflict free within each half warp.  Twiddles come from per-pass tables computed on
 // the host in double precision and rounded to float: the pass with stride NS
 // and radix RP stores W_{NS*RP}^{bm*r} at [r*NS + bm], so the twiddle loads of
-// a warp (consecutive bm) are contiguous.
+// a warp (consecutive bm) are contiguous.  A plan holds the radix-16 tables
+// followed by the radix-8 tables (host_twiddles).
 #pragma once
+
+#include <cmath>
 
 #include "nsgb_common.cuh"
 
@@ -96,27 +101,49 @@ __device__ __forceinline__ void dft(float2 (&a)[R]) {
 }
 
 // Offset (in complex entries) of the twiddle table of the pass with stride
-// NS: the passes before it all have radix 16 and stride 16, 256, ...
+// NS in the radix-R tables: the passes before it all have radix R and stride
+// R, R^2, ...
+template <int R>
 __host__ __device__ constexpr int tw_offset(int NS) {
   int off = 0;
-  for (int ns = 16; ns < NS; ns *= 16) off += 16 * ns;
+  for (int ns = R; ns < NS; ns *= R) off += R * ns;
   return off;
 }
-// Total twiddle entries for length N.
+// Twiddle entries of the radix-R tables for length N.
+template <int R>
 __host__ __device__ constexpr int tw_entries(int N) {
   int off = 0;
-  for (int ns = 16; ns < N; ns *= 16) off += ((N / ns >= 16) ? 16 : N / ns) * ns;
+  for (int ns = R; ns < N; ns *= R) off += ((N / ns >= R) ? R : N / ns) * ns;
   return off > 0 ? off : 1;
+}
+// Entries of a plan's table (radix 16, then radix 8) and the radix-8 offset.
+__host__ __device__ constexpr int tw_total(int N) { return tw_entries<16>(N) + tw_entries<8>(N); }
+__host__ __device__ constexpr int tw8_offset(int N) { return tw_entries<16>(N); }
+
+// Fill a plan's twiddle table (tw_total(N) entries): per pass with stride ns
+// and radix rp, W_{ns*rp}^{bm*r} at [off + r*ns + bm], in double then rounded.
+inline void host_twiddles(int N, float2* out) {
+  for (int i = 0; i < tw_total(N); ++i) out[i] = make_float2(1.f, 0.f);
+  for (int R = 16, base = 0; R >= 8; base += tw_entries<16>(N), R /= 2) {
+    for (int ns = R, off = base; ns < N; off += (N / ns >= R ? R : N / ns) * ns, ns *= R) {
+      const int rp = N / ns >= R ? R : N / ns;
+      for (int r = 1; r < rp; ++r)
+        for (int bm = 0; bm < ns; ++bm) {
+          const double ang = -2.0 * M_PI * (double)bm * r / ((double)ns * rp);
+          out[off + r * ns + bm] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+        }
+    }
+  }
 }
 
 // One Stockham pass (stride NS) and, recursively, the remaining passes.
-template <int N, int NS, bool INV>
-__device__ __forceinline__ void pass(float2 (&a)[ept(N)], float2* __restrict__ sb, int j,
+template <int N, int NS, bool INV, int E>
+__device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, int j,
                                      const float2* __restrict__ tw) {
-  constexpr int E = ept(N);
+  static_assert(E == 16 || E == 8 || E == N, "radix");
   constexpr int T = N / E;
   constexpr int REM = N / NS;
-  constexpr int RP = REM >= 16 ? 16 : REM;
+  constexpr int RP = REM >= E ? E : REM;
   constexpr int Q = E / RP;
   constexpr bool LAST = (NS * RP == N);
 #pragma unroll
@@ -127,7 +154,7 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float2* __restrict__ s
     for (int r = 0; r < RP; ++r) x[r] = a[q + r * Q];
     if constexpr (NS > 1) {
       const int bm = b & (NS - 1);
-      const float2* __restrict__ tp = tw + tw_offset(NS) + bm;
+      const float2* __restrict__ tp = tw + tw_offset<E>(NS) + bm;
 #pragma unroll
       for (int r = 1; r < RP; ++r) {
         float2 w = __ldg(tp + r * NS);
@@ -150,18 +177,18 @@ __device__ __forceinline__ void pass(float2 (&a)[ept(N)], float2* __restrict__ s
 #pragma unroll
     for (int s = 0; s < E; ++s) a[s] = sb[pad(j + s * T)];
     __syncthreads();
-    pass<N, NS * RP, INV>(a, sb, j, tw);
+    pass<N, NS * RP, INV, E>(a, sb, j, tw);
   }
 }
 
-// Full FFT of length N (unnormalised; INV uses exp(+2 pi i ...)).  Every
-// thread of the CTA must call it: it synchronises the block between passes.
-// On return the exchange buffer is free for reuse without a further barrier
-// only after the caller's next __syncthreads.
-template <int N, bool INV>
-__device__ __forceinline__ void block_fft(float2 (&a)[ept(N)], float2* sb, int j,
-                                          const float2* __restrict__ tw) {
-  pass<N, 1, INV>(a, sb, j, tw);
+// Full FFT of length N (unnormalised; INV uses exp(+2 pi i ...)) in radix E,
+// with `tw` the radix-E tables.  Every thread of the CTA must call it: it
+// synchronises the block between passes.  On return the exchange buffer is
+// free for reuse without a further barrier only after the caller's next
+// __syncthreads.
+template <int N, bool INV, int E>
+__device__ __forceinline__ void block_fft(float2 (&a)[E], float2* sb, int j, const float2* __restrict__ tw) {
+  pass<N, 1, INV, E>(a, sb, j, tw);
 }
 
 }  // namespace fft

@@ -36,10 +36,9 @@ __host__ __device__ constexpr int pair_stride() {
 
 // ---------------------------------------------------------------- rows fwd --
 // blockDim = (T, P): P row pairs per CTA, rows [blockIdx.x * 2P, +2P).
-template <int N>
+template <int N, int E>
 __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, float2* __restrict__ spec,
                                               const float2* __restrict__ tw) {
-  constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
   extern __shared__ float2 smem2[];
@@ -54,7 +53,7 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) a[s] = make_float2(__ldcs(ra + j + s * T), __ldcs(rb + j + s * T));
-  fft::block_fft<N, false>(a, sb, j, tw);
+  fft::block_fft<N, false, E>(a, sb, j, tw);
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < E; ++s) sb[pad(j + s * T)] = a[s];
@@ -84,10 +83,9 @@ __device__ __forceinline__ float poisson_mult(float k2x, float k2y, float scale)
 }
 
 // blockDim = (T, KB): KB spectrum rows per CTA, rows [blockIdx.x * KB, +KB).
-template <int N>
+template <int N, int E>
 __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float2* __restrict__ tw,
                                           const float* __restrict__ k2, float scale) {
-  constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
   extern __shared__ float2 smem2[];
@@ -102,7 +100,7 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) a[s] = __ldcs(row + j + s * T);
-  fft::block_fft<N, false>(a, sb, j, tw);
+  fft::block_fft<N, false, E>(a, sb, j, tw);
 
   const float k2y = __ldg(k2 + ky);
 #pragma unroll
@@ -110,7 +108,7 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
     const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
     a[s] = make_float2(a[s].x * g, a[s].y * g);
   }
-  fft::block_fft<N, true>(a, sb, j, tw);
+  fft::block_fft<N, true, E>(a, sb, j, tw);
   __syncthreads();  // rows clamped to N/2 were loaded by other threads
   if (kreq <= H) {
 #pragma unroll
@@ -119,10 +117,9 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
 }
 
 // ---------------------------------------------------------------- rows inv --
-template <int N>
+template <int N, int E>
 __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, float* __restrict__ p,
                                               const float2* __restrict__ tw) {
-  constexpr int E = ept(N);
   constexpr int T = N / E;
   constexpr int H = N / 2;
   extern __shared__ float2 smem2[];
@@ -175,7 +172,7 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     a[s] = z;
   }
   __syncthreads();
-  fft::block_fft<N, true>(a, sb, j, tw);
+  fft::block_fft<N, true, E>(a, sb, j, tw);
   float* ra = p + (size_t)(i0 + 2 * pp) * N;
   float* rb = ra + N;
 #pragma unroll
@@ -186,76 +183,120 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
 }
 
 // ---------------------------------------------------------------- kernels --
-template <int N>
+// Radix 16 keeps about 64 registers per thread; radix 8 about 40, so its
+// column kernel is bounded for three 512-thread CTAs per SM.
+template <int N, int E>
 __global__ void __launch_bounds__(1024) k_rows_fwd(const float* __restrict__ rhs, float2* __restrict__ spec,
                                                    const float2* __restrict__ tw) {
-  rows_fwd_body<N>(rhs, spec, tw);
+  rows_fwd_body<N, E>(rhs, spec, tw);
 }
-template <int N>
-__global__ void __launch_bounds__(512, 2) k_cols(float2* __restrict__ spec, const float2* __restrict__ tw,
-                                              const float* __restrict__ k2, float scale) {
-  cols_body<N>(spec, tw, k2, scale);
+template <int N, int E>
+__global__ void __launch_bounds__(512, E == 8 ? 3 : 2) k_cols(float2* __restrict__ spec,
+                                                              const float2* __restrict__ tw,
+                                                              const float* __restrict__ k2, float scale) {
+  cols_body<N, E>(spec, tw, k2, scale);
 }
-template <int N>
+template <int N, int E>
 __global__ void __launch_bounds__(1024) k_rows_inv(const float2* __restrict__ spec, float* __restrict__ p,
                                                    const float2* __restrict__ tw) {
-  rows_inv_body<N>(spec, p, tw);
+  rows_inv_body<N, E>(spec, p, tw);
 }
 // Ensemble variants: blockIdx.y selects the member.
-template <int N>
+template <int N, int E>
 __global__ void __launch_bounds__(1024) k_rows_fwd_b(const SolveDev* __restrict__ sv,
                                                      const float2* __restrict__ tw) {
   const FftPtrs f = sv[blockIdx.y].fft;
-  rows_fwd_body<N>(f.rhs, f.spec, tw);
+  rows_fwd_body<N, E>(f.rhs, f.spec, tw);
 }
-template <int N>
-__global__ void __launch_bounds__(512, 2) k_cols_b(const SolveDev* __restrict__ sv, const float2* __restrict__ tw,
-                                                const float* __restrict__ k2, float scale) {
-  cols_body<N>(sv[blockIdx.y].fft.spec, tw, k2, scale);
+template <int N, int E>
+__global__ void __launch_bounds__(512, E == 8 ? 3 : 2) k_cols_b(const SolveDev* __restrict__ sv,
+                                                                const float2* __restrict__ tw,
+                                                                const float* __restrict__ k2, float scale) {
+  cols_body<N, E>(sv[blockIdx.y].fft.spec, tw, k2, scale);
 }
-template <int N>
+template <int N, int E>
 __global__ void __launch_bounds__(1024) k_rows_inv_b(const SolveDev* __restrict__ sv,
                                                      const float2* __restrict__ tw) {
   const FftPtrs f = sv[blockIdx.y].fft;
-  rows_inv_body<N>(f.spec, f.p, tw);
+  rows_inv_body<N, E>(f.spec, f.p, tw);
 }
 
 // ------------------------------------------------------------- launchers --
-template <int N>
-static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
-  constexpr int T = N / ept(N);
+template <int N, int E>
+static const float2* radix_tables(const FftLaunch& L) {
+  return L.tw + (E == 8 ? fft::tw8_offset(N) : 0);
+}
+
+template <class K>
+static void allow_smem(K kernel) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+template <int N, int E>
+static cudaError_t stage_rows_fwd(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
+  constexpr int T = N / E;
   const int P = L.rows_per_cta / 2;
-  const int KB = L.cols_per_cta;
-  const size_t smem_rows = (size_t)P * pair_stride<N>() * sizeof(float2);
-  const size_t smem_cols = (size_t)KB * pair_stride<N>() * sizeof(float2);
+  const size_t smem = (size_t)P * pair_stride<N>() * sizeof(float2);
   static bool configured = false;  // per-process attribute set-up (idempotent)
   if (!configured) {
-    const int mx = 200 * 1024;
-    cudaFuncSetAttribute(k_rows_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_cols<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_rows_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_rows_fwd_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_cols_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
-    cudaFuncSetAttribute(k_rows_inv_b<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx);
+    allow_smem(k_rows_fwd<N, E>);
+    allow_smem(k_rows_fwd_b<N, E>);
     configured = true;
   }
-  if (sv) {
-    const dim3 gr(N / (2 * P), count), gc((N / 2) / KB + 1, count);
-    k_rows_fwd_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
-    k_cols_b<N><<<gc, dim3(T, KB), smem_cols, st>>>(sv, L.tw, L.k2, L.scale);
-    k_rows_inv_b<N><<<gr, dim3(T, P), smem_rows, st>>>(sv, L.tw);
-    return cudaGetLastError();
-  }
-  if (L.rhs) {
-    k_rows_fwd<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.rhs, L.spec, L.tw);
-  }
-  if (L.do_cols) {
-    k_cols<N><<<(N / 2) / KB + 1, dim3(T, KB), smem_cols, st>>>(L.spec, L.tw, L.k2, L.scale);
-  }
-  if (L.p) {
-    k_rows_inv<N><<<N / (2 * P), dim3(T, P), smem_rows, st>>>(L.spec, L.p, L.tw);
-  }
+  if (sv)
+    k_rows_fwd_b<N, E><<<dim3(N / (2 * P), count), dim3(T, P), smem, st>>>(sv, radix_tables<N, E>(L));
+  else
+    k_rows_fwd<N, E><<<N / (2 * P), dim3(T, P), smem, st>>>(L.rhs, L.spec, radix_tables<N, E>(L));
   return cudaGetLastError();
+}
+
+template <int N, int E>
+static cudaError_t stage_cols(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
+  constexpr int T = N / E;
+  const int KB = L.cols_per_cta;
+  const size_t smem = (size_t)KB * pair_stride<N>() * sizeof(float2);
+  static bool configured = false;
+  if (!configured) {
+    allow_smem(k_cols<N, E>);
+    allow_smem(k_cols_b<N, E>);
+    configured = true;
+  }
+  if (sv)
+    k_cols_b<N, E><<<dim3((N / 2) / KB + 1, count), dim3(T, KB), smem, st>>>(sv, radix_tables<N, E>(L), L.k2,
+                                                                            L.scale);
+  else
+    k_cols<N, E><<<(N / 2) / KB + 1, dim3(T, KB), smem, st>>>(L.spec, radix_tables<N, E>(L), L.k2, L.scale);
+  return cudaGetLastError();
+}
+
+template <int N, int E>
+static cudaError_t stage_rows_inv(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
+  constexpr int T = N / E;
+  const int P = L.rows_per_cta / 2;
+  const size_t smem = (size_t)P * pair_stride<N>() * sizeof(float2);
+  static bool configured = false;
+  if (!configured) {
+    allow_smem(k_rows_inv<N, E>);
+    allow_smem(k_rows_inv_b<N, E>);
+    configured = true;
+  }
+  if (sv)
+    k_rows_inv_b<N, E><<<dim3(N / (2 * P), count), dim3(T, P), smem, st>>>(sv, radix_tables<N, E>(L));
+  else
+    k_rows_inv<N, E><<<N / (2 * P), dim3(T, P), smem, st>>>(L.spec, L.p, radix_tables<N, E>(L));
+  return cudaGetLastError();
+}
+
+template <int N>
+static cudaError_t launch_poisson_fft(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
+  const bool r8 = L.radix_rows == 8, c8 = L.radix_cols == 8;
+  cudaError_t e = cudaSuccess;
+  if (sv || L.rhs) e = r8 ? stage_rows_fwd<N, 8>(L, sv, count, st) : stage_rows_fwd<N, fft::ept(N)>(L, sv, count, st);
+  if (e == cudaSuccess && (sv || L.do_cols))
+    e = c8 ? stage_cols<N, 8>(L, sv, count, st) : stage_cols<N, fft::ept(N)>(L, sv, count, st);
+  if (e == cudaSuccess && (sv || L.p))
+    e = r8 ? stage_rows_inv<N, 8>(L, sv, count, st) : stage_rows_inv<N, fft::ept(N)>(L, sv, count, st);
+  return e;
 }
 
 size_t fft_rows_smem_bytes(int N, int rows_per_cta) {

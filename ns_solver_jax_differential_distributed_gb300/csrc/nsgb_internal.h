@@ -19,6 +19,8 @@ struct FftLaunch {
   float scale = 0.f;           // 1 / (2 N^2)
   int rows_per_cta = 8;        // even, power of two
   int cols_per_cta = 2;        // power of two
+  int radix_rows = 16;         // Stockham radix of the row passes (16 or 8)
+  int radix_cols = 16;         // ... and of the column pass
 };
 cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st);
 size_t fft_rows_smem_bytes(int N, int rows_per_cta);

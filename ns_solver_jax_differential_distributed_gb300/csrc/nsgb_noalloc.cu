@@ -32,7 +32,7 @@
 namespace {
 
 constexpr int kMaxN = NSGB_NOALLOC_MAX_N;
-constexpr int kMaxTw = nsgb::fft::tw_entries(kMaxN);
+constexpr int kMaxTw = nsgb::fft::tw_total(kMaxN);
 
 static __device__ __align__(256) float2 g_noalloc_spec[(kMaxN / 2 + 1) * kMaxN];
 static __device__ __align__(256) float2 g_noalloc_tw[kMaxTw];
@@ -64,15 +64,7 @@ int fail(int code, const char* fmt, ...) {
 // Twiddles of the Stockham passes and squared wavenumbers, laid out and
 // rounded exactly as a plan of the same (N, L) holds them.
 void fill_tables(int N, double L) {
-  for (int i = 0; i < nsgb::fft::tw_entries(N); ++i) g_host_tw[i] = make_float2(1.f, 0.f);
-  for (int ns = 16, off = 0; ns < N; off += (N / ns >= 16 ? 16 : N / ns) * ns, ns *= 16) {
-    const int rp = N / ns >= 16 ? 16 : N / ns;
-    for (int r = 1; r < rp; ++r)
-      for (int bm = 0; bm < ns; ++bm) {
-        const double ang = -2.0 * M_PI * (double)bm * r / ((double)ns * rp);
-        g_host_tw[off + r * ns + bm] = make_float2((float)std::cos(ang), (float)std::sin(ang));
-      }
-  }
+  nsgb::fft::host_twiddles(N, g_host_tw);
   const double dx = L / N;
   const float dn = (float)(dx * N);
   for (int m = 0; m < N; ++m) {
@@ -120,7 +112,7 @@ extern "C" int nsgb_poisson_noalloc(int N, double L, const float* rhs, float* p,
   fill_tables(N, L);
   // From pageable host memory these copies return once the data is staged,
   // so the static host tables may be refilled by the next call.
-  e = cudaMemcpyToSymbolAsync(g_noalloc_tw, g_host_tw, sizeof(float2) * nsgb::fft::tw_entries(N), 0,
+  e = cudaMemcpyToSymbolAsync(g_noalloc_tw, g_host_tw, sizeof(float2) * nsgb::fft::tw_total(N), 0,
                               cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyToSymbolAsync(g_noalloc_k2, g_host_k2, sizeof(float) * N, 0, cudaMemcpyHostToDevice, st);

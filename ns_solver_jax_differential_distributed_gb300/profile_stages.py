@@ -64,14 +64,18 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--tiles", default="", help="tw,th,rows,cols")
+    ap.add_argument("--radix", default="", help="FFT radix of the row and column passes: rows,cols")
     args = ap.parse_args(argv)
     _build.build()
     dev = torch.device("cuda")
     L = 2 * math.pi
     u0 = torch.from_numpy(spectral_u0(args.N, min(32, args.N // 4), 0)).to(dev)
     th = torch.from_numpy(theta_draw(1e-4, 0)).to(dev)
+    plan = _native.get_plan(args.N, L, dev)
+    if args.radix:
+        plan.set_fft_radix(*[int(x) for x in args.radix.split(",")])
     if args.tiles:
-        _native.get_plan(args.N, L, dev).set_tiles(*[int(x) for x in args.tiles.split(",")])
+        plan.set_tiles(*[int(x) for x in args.tiles.split(",")])
     flush = None if args.no_flush else torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     st = _native.time_stages(u0, th, L, 1e-4, 2.5e-4, args.scheme, args.reps, flush)
     try:
@@ -80,7 +84,7 @@ def main(argv=None):
             peak = float(json.load(f)["hbm_gbs"])
     except Exception:
         peak = 6800.0
-    out = {"N": args.N, "scheme": args.scheme, "tiles": _native.get_plan(args.N, L, dev).tiles(), "stages": {}}
+    out = {"N": args.N, "scheme": args.scheme, "tiles": plan.tiles(), "radix": plan.fft_radix(), "stages": {}}
     for k, ms in st.items():
         gbs = _native.STAGE_BYTES_PER_CELL[k] * args.N * args.N / (ms * 1e-3) / 1e9
         out["stages"][k] = {"ms": round(ms, 5), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 3)}
