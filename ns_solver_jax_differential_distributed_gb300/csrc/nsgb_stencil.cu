@@ -200,40 +200,56 @@ __global__ void __launch_bounds__(256) k_stencil_batch(const SolveDev* __restric
 // A CTA owns the rows [r0, r0 + RH) of a band of W columns (W = N: whole
 // rows, the periodic wrap stays inside the CTA; W < N: one extra group of
 // four halo columns on each side, computed but not stored).  Thread g owns the
-// four consecutive columns of group g (one float4 per field row) and at
-// iteration t
+// four consecutive columns of group g and at iteration t
 //   - finishes the projection of row t:  u(t) = u*(t) - dt grad p, from p rows
-//     t-1, t, t+1 in registers and the two p(t) values of the neighbouring
-//     groups,
+//     t-1, t, t+1,
 //   - forms u*next(t-1) from u(t-2), u(t-1), u(t) (registers) and the edge
 //     values of u(t-1) of the neighbouring groups,
 //   - writes u*next(t-2) and rhs(t-2) = div(u*next)/dt, and adds the row's
 //     objective partial u_x(t-2) f_x.
-// Every per-cell expression is the one k_stencil evaluates, so both kernels
-// give the same bits.  Values from other groups (the first and last column of
-// a group) pass through shared memory, double-buffered by iteration parity,
-// so one barrier per iteration orders them; the rows of iteration t+1 are
-// loaded while iteration t computes.  The i-neighbours never leave registers,
-// which removes most of the shared-memory traffic of the tiled kernel.
+// The input rows (p and u*) arrive in shared-memory rings by per-thread
+// asynchronous copies issued kAhead rows ahead, so the loads of later rows
+// overlap the arithmetic without holding registers; p neighbours come straight
+// from the ring.  Computed values that other groups need (the first and last
+// column of a group of u and u*next_y) pass through small edge arrays,
+// double-buffered by iteration parity; one barrier per iteration orders
+// both.  The i-neighbours of computed rows never leave registers.
 namespace rows {
 
-constexpr int F_P = 0, F_UX = 1, F_UY = 2, F_SY = 3;  // exchanged fields
+constexpr int F_UX = 0, F_UY = 1, F_SY = 2;  // exchanged fields
+constexpr int kAhead = 3;                    // rows copied ahead of use
+constexpr int kPRing = 8;                    // p rows t-1 .. t+1+kAhead (power of two)
+constexpr int kURing = 4;                    // u* rows t .. t+kAhead (power of two)
+static_assert(kPRing >= kAhead + 3 && kURing >= kAhead + 1, "ring depth");
 
 __host__ __device__ inline int band_width(int N, int tw) { return tw < N ? tw : N; }
 __host__ __device__ inline int groups(int N, int W) { return W == N ? N / 4 : W / 4 + 2; }
 __host__ __device__ inline int threads(int N, int W) { return (groups(N, W) + 31) / 32 * 32; }
-// shared memory: edges [2 slots][4 fields][2 sides][G], forcing rows, 32 sums
+// ring row: 4 pad floats, the W + 8 columns from j0 - 4 (W < N) or from -4
+// (W = N, wrapped copies at both ends), 4 pad floats
+__host__ __device__ inline int ring_stride(int W) { return W + 16; }
+// shared memory: rings, edges [2 slots][3 fields][2 sides][G], forcing rows,
+// 32 partial sums
 inline size_t smem_bytes(int N, int W, int RH) {
-  return sizeof(float) * ((size_t)16 * groups(N, W) + RH + 2 + 32);
+  return sizeof(float) * ((size_t)(kPRing + 2 * kURing) * ring_stride(W) + (size_t)12 * groups(N, W) + RH + 2 + 32);
 }
 
-__device__ __forceinline__ float4 ld4(const float* __restrict__ base, size_t off) {
-  return __ldg(reinterpret_cast<const float4*>(base + off));
+__device__ __forceinline__ void cp16(float* dst_smem, const float* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
+               "l"(src)
+               : "memory");
 }
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
+}
+
 __device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
   *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
 }
-__device__ __forceinline__ void unpack(const float4 v, float (&o)[4]) {
+__device__ __forceinline__ void ld4s(const float* s, float (&o)[4]) {
+  const float4 v = *reinterpret_cast<const float4*>(s);
   o[0] = v.x;
   o[1] = v.y;
   o[2] = v.z;
@@ -242,10 +258,8 @@ __device__ __forceinline__ void unpack(const float4 v, float (&o)[4]) {
 
 }  // namespace rows
 
-// PF: rows loaded ahead (1: the rows of iteration t+1 are loaded at t).
-template <int SCHEME, int PF>
+template <int SCHEME>
 __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step_off) {
-  static_assert(PF >= 1 && PF <= 3, "prefetch depth");
   using namespace rows;
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
@@ -264,12 +278,17 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   const bool store = active && (wrap || (g >= 1 && g <= G - 2));
   const int gl = g == 0 ? (wrap ? G - 1 : 0) : g - 1;
   const int gr = g == G - 1 ? (wrap ? 0 : G - 1) : g + 1;
+  const int RS = ring_stride(W);
+  const int bi = 4 + 4 * g + (wrap ? 4 : 0);  // the group's first column in a ring row
 
   extern __shared__ __align__(16) float sm[];
-  float* sE = sm;                  // [slot][field][side][G]
-  float* sF = sm + 16 * G;         // f_x of rows r0-1 .. r1
-  float* sRed = sF + RH + 2;       // per-warp partial sums
-  auto edge = [&](int slot, int f, int side) { return sE + ((slot * 4 + f) * 2 + side) * G; };
+  float* sP = sm;                              // [kPRing][RS]
+  float* sUX = sP + kPRing * RS;               // [kURing][RS]
+  float* sUY = sUX + kURing * RS;              // [kURing][RS]
+  float* sE = sUY + kURing * RS;               // [slot][field][side][G]
+  float* sF = sE + 12 * G;                     // f_x of rows r0-1 .. r1
+  float* sRed = sF + RH + 2;                   // per-warp partial sums
+  auto edge = [&](int slot, int f, int side) { return sE + ((slot * 3 + f) * 2 + side) * G; };
 
   int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
   const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
@@ -284,36 +303,36 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   const float* __restrict__ pp = a.p;
   const float* __restrict__ usx_g = a.us;
   const float* __restrict__ usy_g = a.us + NN;
-  auto row_off = [&](int r) { return (size_t)(r & M) * N + col; };
-
-  // registers: p rows t-1, t, t+1; u* row t; u rows t-1, t-2; u*next x rows
-  // t-3, t-2 and y row t-2 (entering iteration t)
-  float pm[4] = {0, 0, 0, 0}, pc[4] = {0, 0, 0, 0}, pn[4] = {0, 0, 0, 0};
-  float usx[4], usy[4];
-  float u1x[4] = {0, 0, 0, 0}, u1y[4] = {0, 0, 0, 0}, u2x[4] = {0, 0, 0, 0}, u2y[4] = {0, 0, 0, 0};
-  float sx3[4] = {0, 0, 0, 0}, sx2[4] = {0, 0, 0, 0}, sy2[4] = {0, 0, 0, 0};
-  if (has_p) {
-    unpack(ld4(pp, row_off(r0 - 3)), pm);
-    unpack(ld4(pp, row_off(r0 - 2)), pc);
-    unpack(ld4(pp, row_off(r0 - 1)), pn);
-  }
-  unpack(ld4(usx_g, row_off(r0 - 2)), usx);
-  unpack(ld4(usy_g, row_off(r0 - 2)), usy);
-  // queued rows entering iteration t: p(t+2+k), u*(t+1+k), k < PF-1
-  float4 qp[PF], qx[PF], qy[PF];
+  // one copy group: p row `pr` (pr > -1000) and u* row `ur` (ur > -1000)
+  auto issue = [=](int pr, bool do_p, int ur, bool do_u) {
+    if (do_p && has_p) {
+      float* dst = sP + (pr & (kPRing - 1)) * RS;
+      const float* src = pp + (size_t)(pr & M) * N;
+      if (active) cp16(dst + bi, src + col);
+      if (wrap && tid == 0) cp16(dst + 4, src + N - 4);
+      if (wrap && tid == G - 1) cp16(dst + N + 8, src);
+    }
+    if (do_u && active) {
+      const int slot = (ur & (kURing - 1)) * RS + bi;
+      const size_t o = (size_t)(ur & M) * N + col;
+      cp16(sUX + slot, usx_g + o);
+      cp16(sUY + slot, usy_g + o);
+    }
+    cp_commit();
+  };
+  // prologue: p rows r0-3, r0-2, then the groups of iterations r0-2-kAhead ..
+  // r0-3 (p rows r0-1 .., u* rows r0-2 ..); wait for those of iteration r0-2
+  issue(r0 - 3, true, 0, false);
+  issue(r0 - 2, true, 0, false);
 #pragma unroll
-  for (int k = 0; k < PF - 1; ++k) {
-    qp[k] = has_p ? ld4(pp, row_off(r0 + k)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    qx[k] = ld4(usx_g, row_off(r0 - 1 + k));
-    qy[k] = ld4(usy_g, row_off(r0 - 1 + k));
-  }
-  if (active) {
-    const int s = (r0 - 3) & 1;
-    edge(s, F_P, 0)[g] = pc[0];
-    edge(s, F_P, 1)[g] = pc[3];
-  }
+  for (int k = kAhead; k >= 1; --k) issue(r0 - 1 - k + kAhead, true, r0 - 2 - k + kAhead, true);
+  cp_wait<kAhead - 1>();
   __syncthreads();
 
+  // registers entering iteration t: u rows t-1, t-2; u*next x rows t-3, t-2
+  // and y row t-2
+  float u1x[4] = {0, 0, 0, 0}, u1y[4] = {0, 0, 0, 0}, u2x[4] = {0, 0, 0, 0}, u2y[4] = {0, 0, 0, 0};
+  float sx3[4] = {0, 0, 0, 0}, sx2[4] = {0, 0, 0, 0}, sy2[4] = {0, 0, 0, 0};
   float jacc = 0.0f;
   float* __restrict__ uso_x = a.us_out;
   float* __restrict__ uso_y = a.us_out + NN;
@@ -321,25 +340,26 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
 #pragma unroll 1
   for (int t = r0 - 2; t <= r1 + 1; ++t) {
     const int rs = (t - 1) & 1, ws = t & 1;
-    // rows of iteration t + PF
-    qp[PF - 1] = has_p ? ld4(pp, row_off(t + 1 + PF)) : make_float4(0.f, 0.f, 0.f, 0.f);
-    qx[PF - 1] = ld4(usx_g, row_off(t + PF));
-    qy[PF - 1] = ld4(usy_g, row_off(t + PF));
+    issue(t + 1 + kAhead, true, t + kAhead, true);
 
     // u(t): projection of row t
     float ux[4], uy[4];
+    {
+      const float* ur = sUX + (t & (kURing - 1)) * RS + bi;
+      ld4s(ur, ux);
+      ld4s(sUY + (t & (kURing - 1)) * RS + bi, uy);
+    }
     if (has_p) {
-      const float P[6] = {edge(rs, F_P, 1)[gl], pc[0], pc[1], pc[2], pc[3], edge(rs, F_P, 0)[gr]};
+      float pm[4], pn[4], q[4];
+      ld4s(sP + ((t - 1) & (kPRing - 1)) * RS + bi, pm);
+      ld4s(sP + ((t + 1) & (kPRing - 1)) * RS + bi, pn);
+      const float* pc = sP + (t & (kPRing - 1)) * RS + bi;
+      ld4s(pc, q);
+      const float P[6] = {pc[-1], q[0], q[1], q[2], q[3], pc[4]};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        ux[k] = fused_proj(usx[k], pn[k], pm[k], c.cP);
-        uy[k] = fused_proj(usy[k], P[k + 2], P[k], c.cP);
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        ux[k] = usx[k];
-        uy[k] = usy[k];
+        ux[k] = fused_proj(ux[k], pn[k], pm[k], c.cP);
+        uy[k] = fused_proj(uy[k], P[k + 2], P[k], c.cP);
       }
     }
 
@@ -364,7 +384,7 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
 #pragma unroll
       for (int k = 0; k < 4; ++k) rh[k] = fused_rhs(sx1[k], sx3[k], Y2[k + 2], Y2[k], c.cD);
       if (store) {
-        const size_t o = row_off(t - 2);
+        const size_t o = (size_t)((t - 2) & M) * N + col;
         st4(uso_x, o, sx2);
         st4(uso_y, o, sy2);
         st4(rhs_g, o, rh);
@@ -378,10 +398,8 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       }
     }
 
-    // edge values for the next iteration: p(t+1), u(t), u*next_y(t-1)
+    // edge values for the next iteration: u(t), u*next_y(t-1)
     if (active) {
-      edge(ws, F_P, 0)[g] = pn[0];
-      edge(ws, F_P, 1)[g] = pn[3];
       edge(ws, F_UX, 0)[g] = ux[0];
       edge(ws, F_UX, 1)[g] = ux[3];
       edge(ws, F_UY, 0)[g] = uy[0];
@@ -391,8 +409,6 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      pm[k] = pc[k];
-      pc[k] = pn[k];
       u2x[k] = u1x[k];
       u2y[k] = u1y[k];
       u1x[k] = ux[k];
@@ -401,17 +417,10 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       sx2[k] = sx1[k];
       sy2[k] = sy1[k];
     }
-    unpack(qp[0], pn);
-    unpack(qx[0], usx);
-    unpack(qy[0], usy);
-#pragma unroll
-    for (int k = 0; k < PF - 1; ++k) {
-      qp[k] = qp[k + 1];
-      qx[k] = qx[k + 1];
-      qy[k] = qy[k + 1];
-    }
+    cp_wait<kAhead - 1>();  // the rows of iteration t+1 have landed
     __syncthreads();
   }
+  cp_wait<0>();
 
   // objective partial of the CTA
   jacc = warp_sum(jacc);
@@ -428,17 +437,15 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   }
 }
 
-constexpr int kRowsPrefetch = 1;
-
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows(const StencilArgs a) {
-  stencil_rows_body<SCHEME, kRowsPrefetch>(a, 0);
+  stencil_rows_body<SCHEME>(a, 0);
 }
 
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows_batch(const SolveDev* __restrict__ solves, int variant,
                                                               int step_off) {
-  stencil_rows_body<SCHEME, kRowsPrefetch>(solves[blockIdx.z].st[variant], step_off);
+  stencil_rows_body<SCHEME>(solves[blockIdx.z].st[variant], step_off);
 }
 
 bool stencil_rows_mode(int tw) { return tw >= NSGB_ROWS_MIN_W; }
