@@ -61,9 +61,10 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
 
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
+  const int lrb = __ffs(RB) - 1;  // RB is a power of two
   for (int e = tid; e < RB * (H + 1); e += nth) {
     const int r = e & (RB - 1);
-    const int k = e / RB;
+    const int k = e >> lrb;
     const float2* pb = smem2 + (r >> 1) * pair_stride<N>();
     const int kn = (N - k) & (N - 1);
     const float2 zk = pb[pad(k)], wk = pb[pad(kn)];
@@ -133,12 +134,13 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   // and X_b[k] at H + 1 + k, k = 0..H.  The strided loads are issued in
   // batches of 8 before their shared-memory stores, so their latencies overlap.
   const int tot = RB * (H + 1);
+  const int lrb = __ffs(RB) - 1;  // RB is a power of two
   auto stage = [&](int e, float2 v) {
     const int r = e & (RB - 1);
-    const int k = e / RB;
+    const int k = e >> lrb;
     smem2[(r >> 1) * pair_stride<N>() + pad((r & 1) * (H + 1) + k)] = v;
   };
-  auto src = [&](int e) { return spec + (size_t)(e / RB) * N + i0 + (e & (RB - 1)); };
+  auto src = [&](int e) { return spec + (size_t)(e >> lrb) * N + i0 + (e & (RB - 1)); };
   int e = tid;
   for (; e + 7 * nth < tot; e += 8 * nth) {
     float2 v[8];
