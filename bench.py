@@ -88,7 +88,7 @@ def max_over_ranks(dist, x: float, device=None) -> float:
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """nvidia-smi samples every 50 ms while the timed region runs."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -105,7 +105,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+                 "-lms", "50"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
@@ -142,16 +142,19 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU baseline
-def cpu_baseline(w, sample_steps: int = 2) -> dict:
+def cpu_baseline(w, target_s: float = 10.0) -> dict:
     """The float32 oracle (restatement of the reference algorithm) on the
-    host: `sample_steps` solver steps of the same N=4096 workload after one
-    warm-up step, FFTs on all host cores (scipy.fft workers)."""
+    host: about `target_s` seconds of solver steps of the same N=4096 workload
+    (step count from a timed warm-up step), FFTs on all host cores (scipy.fft
+    workers)."""
     from oracle import ns_oracle as O
     cores = len(os.sched_getaffinity(0))
     O.set_fft_workers(cores)
     u0, th = w.u0(), w.theta()
     cfg = O.OracleConfig(N=w.N, L=w.L, nu=w.nu, dt=w.dt, steps=w.steps, scheme=w.scheme)
+    t0 = time.perf_counter()
     O.rollout(u0, th, cfg, steps=1)
+    sample_steps = int(max(2, min(40, target_s / max(time.perf_counter() - t0, 1e-3))))
     t0 = time.perf_counter()
     O.rollout(u0, th, cfg, steps=sample_steps)
     dt_s = time.perf_counter() - t0
@@ -170,18 +173,21 @@ def measured_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (a line 'traffic <kernel> <N> <bytes>' in profiles/ncu_summary.md)."""
-    path = os.path.join(ROOT, "profiles", "ncu_summary.md")
+def ncu_traffic(stage: str, N: int = 4096):
+    """DRAM bytes (read + write) per launch of a stage's kernel at size N, from
+    the committed ncu summaries: a line 'traffic <stage> <N> <bytes>' in a
+    profiles/*.md file."""
+    d = os.path.join(ROOT, "profiles")
     try:
-        with open(path) as f:
+        names = sorted(f for f in os.listdir(d) if f.endswith(".md"))
+    except OSError:
+        return None
+    for name in names:
+        with open(os.path.join(d, name)) as f:
             for line in f:
                 parts = line.strip().strip("`").split()
-                if len(parts) == 4 and parts[0] == "traffic" and parts[1] == kernel and parts[2] == "4096":
+                if len(parts) == 4 and parts[0] == "traffic" and parts[1] == stage and parts[2] == str(N):
                     return float(parts[3])
-    except OSError:
-        pass
     return None
 
 
@@ -301,7 +307,8 @@ def run_ours(args, world, rank, local):
                        "nu": w.nu, "scheme": w.scheme, "L": "2pi", "u0": f"seeded spectral |k|<={w.K}",
                        "theta": "[A,B,nu] within 20% of [1,0.5,nu]", "parallelism": f"replicas{world}",
                        "l2": "working set ~470 MB > L2 (no flush needed)",
-                       "tiles": {k: tiles[k] for k in ("tw", "th", "rows", "cols")},
+                       "tiles": {k: tiles.get(k, 16) for k in ("tw", "th", "rows", "cols", "radix_rows",
+                                                                "radix_cols")},
                        "cell_steps_per_step": int(cells)},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
             "gpu_launches": launches_per_rollout(w.steps, True) * args.steps,
@@ -330,7 +337,7 @@ def run_reference(args, world, rank):
     cfg = O.OracleConfig(N=w.N, L=w.L, nu=w.nu, dt=w.dt, steps=w.steps, scheme=w.scheme)
     warm = max(1, min(args.warmup, 2))
     O.rollout(u0, th, cfg, steps=warm)
-    steps = max(1, min(args.steps, 5))
+    steps = max(1, min(args.steps, 40))  # one solver step per bench step, bounded
     t0 = time.perf_counter()
     O.rollout(u0, th, cfg, steps=steps)
     el = time.perf_counter() - t0
