@@ -355,9 +355,13 @@ def run_reference(args, world, rank):
 # ------------------------------------------------- the systems workloads
 def run_grad(args):
     """Differentiation: dJ/dtheta by the discrete adjoint, N=1024, 1000 steps,
-    dt=1e-3, nu=5e-4, upwind, checkpoints every 50 steps; time against the
-    forward rollout, peak memory, and central finite differences of the GPU
-    forward (relative steps 1e-4 for A, 1e-3 for B and nu)."""
+    dt=1e-3, nu=5e-4, upwind; time against the forward rollout and peak memory
+    with checkpoints every 50 steps (recompute in the backward pass) and with
+    the automatic policy (every state kept when the states fit in half the
+    free HBM: 8.4 GB here, no recompute); central finite differences of the
+    GPU float32 forward as a sanity check (relative steps 1e-4 for A, 1e-3
+    for B, 5e-2 for nu, whose sensitivity is below float32 resolution at
+    smaller steps)."""
     import torch
     import ns_solver_jax_differential_distributed_gb300 as nsgb
     from ns_solver_jax_differential_distributed_gb300 import _build, autotune
@@ -388,10 +392,16 @@ def run_grad(args):
     torch.cuda.reset_peak_memory_stats(dev)
     t_grad, (Jg, g) = timed(lambda: solver.gradient(u0, th), max(1, args.steps))
     mem_grad = torch.cuda.max_memory_allocated(dev)
+    solver_all = nsgb.SingleCoreNSSolver(nsgb.make_grid(w.N, w.L), nsgb.Phys(nu=w.nu, mu0=0.5, sigma0=0.1, C=1.0),
+                                         nsgb.Time(dt=w.dt, steps=w.steps), w.scheme, device=dev)
+    every_auto = solver_all._every()
+    torch.cuda.reset_peak_memory_stats(dev)
+    t_all, (_, g_all) = timed(lambda: solver_all.gradient(u0, th), max(1, args.steps))
+    mem_all = torch.cuda.max_memory_allocated(dev)
     g = g.double().cpu().numpy()
     th64 = th.double().cpu().numpy()
     fd = []
-    for k, rs in enumerate((1e-4, 1e-3, 1e-3)):
+    for k, rs in enumerate((1e-4, 1e-3, 5e-2)):
         h = rs * abs(th64[k])
         tp, tm = th64.copy(), th64.copy()
         tp[k] += h
@@ -406,6 +416,9 @@ def run_grad(args):
             "forward_cell_steps_per_s": cells / (t_fwd / 1e3), "J": float(Jg), "dJdtheta": g.tolist(),
             "fd_gpu_float32": fd, "fd_rel_diff": [abs(a - b) / max(abs(b), 1e-30) for a, b in zip(g, fd)],
             "peak_mem_forward_bytes": mem_fwd, "peak_mem_gradient_bytes": mem_grad,
+            "auto_checkpoint": {"checkpoint_every": every_auto, "gradient_ms": t_all,
+                                "ratio_to_forward": t_all / t_fwd, "peak_mem_gradient_bytes": mem_all,
+                                "max_abs_diff_vs_every_50": float(np.abs(g_all.double().cpu().numpy() - g).max())},
             "dtype": "f32", "data": "synthetic"}
 
 

@@ -6,8 +6,9 @@ cold L2 for grids larger than L2) and keeps the fastest per stage:
 
 * stencil launch shape: a tile (width x height cells) of the tiled kernel or
   a band (width x rows) of the row-streaming kernel,
-* rows per CTA of the row FFTs (forward and inverse),
-* spectrum rows per CTA of the column FFT.
+* Stockham radix (16 or 8) and rows per CTA of the row FFTs (forward and
+  inverse),
+* Stockham radix and spectrum rows per CTA of the column FFT.
 
 Results are cached in a JSON file keyed by GPU name, N and scheme
 (``$NSGB_TUNE_CACHE`` or ``<package>/_autotune/tiles.json``) so a process
@@ -33,6 +34,7 @@ _lock = threading.Lock()
 STENCIL_TILES = [(16, 8), (16, 16), (32, 8), (32, 16), (64, 8), (64, 16), (128, 8)]
 ROW_CHOICES = [2, 4, 8, 16]
 COL_CHOICES = [1, 2, 4]
+RADIX_CHOICES = [16, 8]
 
 
 def _load() -> dict:
@@ -77,13 +79,22 @@ def row_band_shapes(N: int, sms: int) -> list:
 
 
 def candidates(N: int, sms: int = 152) -> dict:
-    T = N // min(16, N)
     st = [(w, h) for (w, h) in STENCIL_TILES if w <= N and h <= N]
     if N >= 256:
         st += row_band_shapes(N, sms)
-    rows = [r for r in ROW_CHOICES if r <= N and (r // 2) * T <= 1024]
-    cols = [c for c in COL_CHOICES if c <= N // 2 and c * T <= 512]
+    rows, cols = [], []
+    for radix in RADIX_CHOICES:
+        T = N // min(radix, N)
+        rows += [(radix, r) for r in ROW_CHOICES if r <= N and (r // 2) * T <= 1024]
+        cols += [(radix, c) for c in COL_CHOICES if c <= N // 2 and c * T <= 512]
     return {"stencil": st, "rows": rows, "cols": cols}
+
+
+def _apply(plan, best: dict) -> None:
+    # radix first at shapes valid for both radices, then the tuned shapes
+    plan.set_tiles(best["tw"], best["th"], 2, 1)
+    plan.set_fft_radix(best.get("radix_rows", 16), best.get("radix_cols", 16))
+    plan.set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
 
 
 def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, reps: int = 5,
@@ -96,7 +107,7 @@ def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, r
         cache = _load()
         if key in cache and not force:
             best = cache[key]
-            plan.set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
+            _apply(plan, best)
             return best
     from .workloads import spectral_u0
     u0 = torch.from_numpy(spectral_u0(N, min(32, N // 4), 0)).to(device)
@@ -106,25 +117,32 @@ def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, r
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device) if cells * 28 > (96 << 20) else None
     cand = candidates(N, torch.cuda.get_device_properties(device).multi_processor_count)
     base = plan.tiles()
+    base_radix = plan.fft_radix()
     results = {"stencil": {}, "rows": {}, "cols": {}}
     for (w, h) in cand["stencil"]:
         plan.set_tiles(w, h, base[2], base[3])
         results["stencil"][(w, h)] = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)["stencil"]
-    for r in cand["rows"]:
-        plan.set_tiles(base[0], base[1], r, base[3])
+    # FFT shapes: each (radix, CTA shape) of one pass with the other pass at
+    # its smallest shape, which every radix accepts
+    for (radix, r) in cand["rows"]:
+        plan.set_tiles(base[0], base[1], 2, 1)
+        plan.set_fft_radix(radix, 16)
+        plan.set_tiles(base[0], base[1], r, 1)
         t = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)
-        results["rows"][r] = t["rows_fwd"] + t["rows_inv"]
-    for c in cand["cols"]:
-        plan.set_tiles(base[0], base[1], base[2], c)
-        results["cols"][c] = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)["cols"]
+        results["rows"][(radix, r)] = t["rows_fwd"] + t["rows_inv"]
+    for (radix, c) in cand["cols"]:
+        plan.set_tiles(base[0], base[1], 2, 1)
+        plan.set_fft_radix(16, radix)
+        plan.set_tiles(base[0], base[1], 2, c)
+        results["cols"][(radix, c)] = _native.time_stages(u0, th, L, nu, dt, scheme, reps, flush)["cols"]
     tw, thh = min(results["stencil"], key=results["stencil"].get)
-    rows = min(results["rows"], key=results["rows"].get)
-    cols = min(results["cols"], key=results["cols"].get)
-    plan.set_tiles(tw, thh, rows, cols)
-    best = {"tw": tw, "th": thh, "rows": rows, "cols": cols,
-            "ms": {"stencil": results["stencil"][(tw, thh)], "rows_fwd+inv": results["rows"][rows],
-                   "cols": results["cols"][cols]},
-            "default": list(base)}
+    rr, rows = min(results["rows"], key=results["rows"].get)
+    rc, cols = min(results["cols"], key=results["cols"].get)
+    best = {"tw": tw, "th": thh, "rows": rows, "cols": cols, "radix_rows": rr, "radix_cols": rc,
+            "ms": {"stencil": results["stencil"][(tw, thh)], "rows_fwd+inv": results["rows"][(rr, rows)],
+                   "cols": results["cols"][(rc, cols)]},
+            "default": list(base) + list(base_radix)}
+    _apply(plan, best)
     if verbose:
         print(f"autotune N={N} {scheme}: best {best}")
         for kind, res in results.items():
@@ -142,5 +160,5 @@ def apply_cached(N: int, L: float, scheme: str, device=None) -> bool:
     best = _load().get(_key(N, scheme, device))
     if not best:
         return False
-    _native.get_plan(N, L, device).set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
+    _apply(_native.get_plan(N, L, device), best)
     return True

@@ -20,59 +20,89 @@
 //   + (1 - m_{i-1}) w_{i-1}] / dx.
 // The projection Pr lambda_{s+1} reuses the forward machinery: the previous
 // adjoint kernel wrote rhs = div(lambda_{s+1}) / dt, the FFT kernels solved for
-// p, and this kernel applies mu = lambda - dt grad p on its tile.
+// p, and this kernel applies mu = lambda - dt grad p on its tile.  The cell
+// arithmetic uses the folded coefficients of the fused forward step (dt/h,
+// dt nu/dx^2, 1/(h dt)) and FMAs; the theta sensitivities are summed in float
+// over a thread's few cells and in double from there on.
 #include "nsgb_internal.h"
 
 namespace nsgb {
 
+// Shared-memory planes of one TW x TH tile: p with a 3-cell halo, u and
+// lambda with a 2-cell halo, all fetched as aligned float4 groups from column
+// j0 - 4 (pitch W4 = TW + 8), then lambda_s on the tile + 1 halo (pitch SW).
+template <int TW, int TH>
+struct AdjointSmem {
+  static constexpr int G = TW / 4 + 2;
+  static constexpr int W4 = 4 * G;
+  static constexpr int PH = TH + 6, UH = TH + 4, SH = TH + 2, SW = TW + 2;
+  static constexpr int P_OFF = 0;
+  static constexpr int UX_OFF = P_OFF + PH * W4;
+  static constexpr int UY_OFF = UX_OFF + UH * W4;
+  static constexpr int MX_OFF = UY_OFF + UH * W4;
+  static constexpr int MY_OFF = MX_OFF + UH * W4;
+  static constexpr int LX_OFF = MY_OFF + UH * W4;
+  static constexpr int LY_OFF = LX_OFF + SH * SW;
+  static constexpr int F_OFF = LY_OFF + SH * SW;  // fx for the SH rows
+  static constexpr int DA_OFF = F_OFF + SH;        // dfx/dA, dfx/dB for the TH rows
+  static constexpr int DB_OFF = DA_OFF + TH;
+  static constexpr int RED_OFF = (DB_OFF + TH + 1) & ~1;  // 24 doubles
+  static constexpr size_t BYTES = (size_t)RED_OFF * sizeof(float) + 24 * sizeof(double);
+};
+
 template <int SCHEME, int TW, int TH>
 __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
-  extern __shared__ float sm[];
+  using Lay = AdjointSmem<TW, TH>;
+  constexpr int G = Lay::G, W4 = Lay::W4, PH = Lay::PH, UH = Lay::UH, SH = Lay::SH, SW = Lay::SW;
+  extern __shared__ __align__(16) float sm[];
+  float* sP = sm + Lay::P_OFF;
+  float* sUx = sm + Lay::UX_OFF;
+  float* sUy = sm + Lay::UY_OFF;
+  float* sMx = sm + Lay::MX_OFF;
+  float* sMy = sm + Lay::MY_OFF;
+  float* sLx = sm + Lay::LX_OFF;
+  float* sLy = sm + Lay::LY_OFF;
+  float* sF = sm + Lay::F_OFF;
+  float* sDA = sm + Lay::DA_OFF;
+  float* sDB = sm + Lay::DB_OFF;
+  double* sRed = reinterpret_cast<double*>(sm + Lay::RED_OFF);
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
   const size_t NN = (size_t)N * N;
   const int j0 = blockIdx.x * TW, i0 = blockIdx.y * TH;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * 32 + tx;
-  constexpr int PW = TW + 6, PH = TH + 6;
-  constexpr int UW = TW + 4, UH = TH + 4;
-  constexpr int SW = TW + 2, SH = TH + 2;
-  float* sP = sm;
-  float* sMx = sP + PH * PW;
-  float* sMy = sMx + UH * UW;
-  float* sUx = sMy + UH * UW;
-  float* sUy = sUx + UH * UW;
-  float* sLx = sUy + UH * UW;
-  float* sLy = sLx + SH * SW;
-  float* sF = sLy + SH * SW;   // fx for the SH rows of the lambda tile
-  float* sDA = sF + SH;        // dfx/dA for the TH interior rows
-  float* sDB = sDA + TH;       // dfx/dB
-  double* sRed = reinterpret_cast<double*>(sDB + TH + ((TH & 1) ? 1 : 0));  // 3 x 8 doubles
 
   const float dt = c.dt;
   const float jscale = c.jscale;  // float32(dt * dx^2) = dJ/du_x / f_x
   const float nu = (a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float cL = fmul(c.dtdx2, nu);                              // dt nu / dx^2
+  const float cA = SCHEME == NSGB_SCHEME_CENTRAL ? c.cAc : c.cAu;  // dt / h
   const float t = fmul((float)a.step, dt);
   const float A = __ldg(a.theta), B = __ldg(a.theta + 1);
 
   const bool has_lam = a.lam != nullptr;
   const bool has_p = a.p != nullptr;
+  // aligned float4 tile loads (a group never straddles the periodic wrap)
   if (has_p) {
     const float* __restrict__ pp = a.p;
-    forflat<PH, PW>(tid, [&](int r, int cc) {
-      sP[r * PW + cc] = __ldg(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 3 + cc) & M));
+    forflat<PH, G>(tid, [&](int r, int q) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(
+          pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M)));
+      *reinterpret_cast<float4*>(sP + r * W4 + 4 * q) = v;
     });
   }
   {
     const float* __restrict__ u = a.u;
     const float* __restrict__ lam = a.lam;
-    forflat<UH, UW>(tid, [&](int r, int cc) {
-      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 2 + cc) & M);
-      const int o = r * UW + cc;
-      sUx[o] = __ldg(u + g);
-      sUy[o] = __ldg(u + NN + g);
-      sMx[o] = has_lam ? __ldg(lam + g) : 0.0f;
-      sMy[o] = has_lam ? __ldg(lam + NN + g) : 0.0f;
+    forflat<UH, G>(tid, [&](int r, int q) {
+      const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 4 + 4 * q) & M);
+      const int o = r * W4 + 4 * q;
+      *reinterpret_cast<float4*>(sUx + o) = __ldg(reinterpret_cast<const float4*>(u + g));
+      *reinterpret_cast<float4*>(sUy + o) = __ldg(reinterpret_cast<const float4*>(u + NN + g));
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<float4*>(sMx + o) = has_lam ? __ldg(reinterpret_cast<const float4*>(lam + g)) : z;
+      *reinterpret_cast<float4*>(sMy + o) = has_lam ? __ldg(reinterpret_cast<const float4*>(lam + NN + g)) : z;
     });
   }
   {
@@ -94,74 +124,79 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
   __syncthreads();
 
-  if (has_p) {  // mu = lambda - dt grad p
-    forflat<UH, UW>(tid, [&](int r, int cc) {
-      const int op = (r + 1) * PW + (cc + 1);
-      const float px = fdiv(fsub(sP[op + PW], sP[op - PW]), c.h2);
-      const float py = fdiv(fsub(sP[op + 1], sP[op - 1]), c.h2);
-      const int o = r * UW + cc;
-      sMx[o] = fsub(sMx[o], fmul(dt, px));
-      sMy[o] = fsub(sMy[o], fmul(dt, py));
+  // mu = lambda - dt grad p on rows i0-2 .. i0+TH+1, columns j0-2 .. j0+TW+1
+  if (has_p) {
+    forflat<UH, TW + 4>(tid, [&](int r, int cc) {
+      const int col = cc + 2;
+      const float* P0 = sP + (r + 1) * W4 + col;
+      const int o = r * W4 + col;
+      sMx[o] = fused_proj(sMx[o], P0[W4], P0[-W4], c.cP);
+      sMy[o] = fused_proj(sMy[o], P0[1], P0[-1], c.cP);
     });
     __syncthreads();
   }
 
-  // theta sensitivities on the interior cells, accumulated in double: the
-  // nu term is a small difference of large contributions
-  double gA = 0.0, gB = 0.0, gN = 0.0;
+  // theta sensitivities of the interior cells: float over a thread's few
+  // cells, double across threads, blocks and steps (the nu term is a small
+  // difference of large contributions)
+  float fA = 0.f, fB = 0.f, fN = 0.f;
   forflat<TH, TW>(tid, [&](int r, int cc) {
-    const int o = (r + 2) * UW + (cc + 2);
-    const float w = jscale * sUx[o] + dt * sMx[o];
-    gA += (double)(w * sDA[r]);
-    gB += (double)(w * sDB[r]);
-    const float lux = (sUx[o - UW] + sUx[o + UW] + sUx[o + 1] + sUx[o - 1] - 4.0f * sUx[o]) / c.dx2;
-    const float luy = (sUy[o - UW] + sUy[o + UW] + sUy[o + 1] + sUy[o - 1] - 4.0f * sUy[o]) / c.dx2;
-    gN += (double)dt * ((double)sMx[o] * lux + (double)sMy[o] * luy);
+    const int o = (r + 2) * W4 + (cc + 4);
+    const float w = fmaf(jscale, sUx[o], dt * sMx[o]);
+    fA = fmaf(w, sDA[r], fA);
+    fB = fmaf(w, sDB[r], fB);
+    // Laplacian sums from neighbour differences: for a smooth field each
+    // difference of close values is exact, so the small sum keeps its digits
+    // (summing the neighbours first would cancel about two of them)
+    const float ox = sUx[o], oy = sUy[o];
+    const float lux = ((sUx[o - W4] - ox) + (sUx[o + W4] - ox)) + ((sUx[o + 1] - ox) + (sUx[o - 1] - ox));
+    const float luy = ((sUy[o - W4] - oy) + (sUy[o + W4] - oy)) + ((sUy[o + 1] - oy) + (sUy[o - 1] - oy));
+    fN = fmaf(sMx[o], lux, fmaf(sMy[o], luy, fN));
   });
+  double gA = (double)fA, gB = (double)fB, gN = (double)fN * ((double)dt * (double)c.rdx2);
 
-  // lambda_s on the tile + 1 halo
-  const float inv_h2 = 1.0f / c.h2;
-  const float inv_h1 = 1.0f / c.h1;
+  // lambda_s on rows i0-1 .. i0+TH, columns j0-1 .. j0+TW
   forflat<SH, SW>(tid, [&](int r, int cc) {
-    const int o = (r + 1) * UW + (cc + 1);
-    const int n = o + UW, s = o - UW, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
+    const int o = (r + 1) * W4 + (cc + 3);
+    const int n = o + W4, s = o - W4, e = o + 1, w = o - 1;  // i+1, i-1, j+1, j-1
     const float mx = sMx[o], my = sMy[o];
-    const float lmx = (sMx[s] + sMx[n] + sMx[e] + sMx[w] - 4.0f * mx) / c.dx2;
-    const float lmy = (sMy[s] + sMy[n] + sMy[e] + sMy[w] - 4.0f * my) / c.dx2;
+    const float lmx = fmaf(-4.0f, mx, (sMx[s] + sMx[n]) + (sMx[e] + sMx[w]));
+    const float lmy = fmaf(-4.0f, my, (sMy[s] + sMy[n]) + (sMy[e] + sMy[w]));
+    // at = h (A'(u)^T mu): the difference quotients' 1/h is folded into cA
     float atx, aty;
     if (SCHEME == NSGB_SCHEME_CENTRAL) {
-      const float gxux = (sUx[n] - sUx[s]) * inv_h2, gxuy = (sUy[n] - sUy[s]) * inv_h2;
-      const float gyux = (sUx[e] - sUx[w]) * inv_h2, gyuy = (sUy[e] - sUy[w]) * inv_h2;
-      atx = -(mx * gxux + my * gxuy) + (sMx[n] * sUx[n] - sMx[s] * sUx[s]) * inv_h2 +
-            (sMx[e] * sUy[e] - sMx[w] * sUy[w]) * inv_h2;
-      aty = -(mx * gyux + my * gyuy) + (sMy[n] * sUx[n] - sMy[s] * sUx[s]) * inv_h2 +
-            (sMy[e] * sUy[e] - sMy[w] * sUy[w]) * inv_h2;
+      const float gxux = sUx[n] - sUx[s], gxuy = sUy[n] - sUy[s];
+      const float gyux = sUx[e] - sUx[w], gyuy = sUy[e] - sUy[w];
+      atx = -fmaf(mx, gxux, my * gxuy) +
+            (fmaf(sMx[n], sUx[n], -sMx[s] * sUx[s]) + fmaf(sMx[e], sUy[e], -sMx[w] * sUy[w]));
+      aty = -fmaf(mx, gyux, my * gyuy) +
+            (fmaf(sMy[n], sUx[n], -sMy[s] * sUx[s]) + fmaf(sMy[e], sUy[e], -sMy[w] * sUy[w]));
     } else {
       const float uxo = sUx[o], uyo = sUy[o];
       const bool mxo = uxo >= 0.f, myo = uyo >= 0.f;
       // one-sided differences of u at o (the forward's dfx, dfy)
-      const float dxux = (mxo ? uxo - sUx[s] : sUx[n] - uxo) * inv_h1;
-      const float dxuy = (mxo ? uyo - sUy[s] : sUy[n] - uyo) * inv_h1;
-      const float dyux = (myo ? uxo - sUx[w] : sUx[e] - uxo) * inv_h1;
-      const float dyuy = (myo ? uyo - sUy[w] : sUy[e] - uyo) * inv_h1;
-      atx = -(mx * dxux + my * dxuy);
-      aty = -(mx * dyux + my * dyuy);
-      // transposed one-sided operators applied to w = mu_c u_x (x) and mu_c u_y (y)
+      const float dxux = mxo ? uxo - sUx[s] : sUx[n] - uxo;
+      const float dxuy = mxo ? uyo - sUy[s] : sUy[n] - uyo;
+      const float dyux = myo ? uxo - sUx[w] : sUx[e] - uxo;
+      const float dyuy = myo ? uyo - sUy[w] : sUy[e] - uyo;
+      atx = -fmaf(mx, dxux, my * dxuy);
+      aty = -fmaf(mx, dyux, my * dyuy);
+      // transposed one-sided operators applied to mu_c u_x (x) and mu_c u_y (y)
       const bool mxn = sUx[n] >= 0.f, mxs = sUx[s] >= 0.f;
       const bool mye = sUy[e] >= 0.f, myw = sUy[w] >= 0.f;
       auto dxt = [&](const float* mu) {
-        return ((mxo ? mu[o] * uxo : -mu[o] * uxo) - (mxn ? mu[n] * sUx[n] : 0.f) +
-                (mxs ? 0.f : mu[s] * sUx[s])) * inv_h1;
+        return (mxo ? mu[o] * uxo : -mu[o] * uxo) - (mxn ? mu[n] * sUx[n] : 0.f) +
+               (mxs ? 0.f : mu[s] * sUx[s]);
       };
       auto dyt = [&](const float* mu) {
-        return ((myo ? mu[o] * uyo : -mu[o] * uyo) - (mye ? mu[e] * sUy[e] : 0.f) +
-                (myw ? 0.f : mu[w] * sUy[w])) * inv_h1;
+        return (myo ? mu[o] * uyo : -mu[o] * uyo) - (mye ? mu[e] * sUy[e] : 0.f) +
+               (myw ? 0.f : mu[w] * sUy[w]);
       };
       atx -= dxt(sMx) + dyt(sMx);
       aty -= dxt(sMy) + dyt(sMy);
     }
-    sLx[r * SW + cc] = mx + dt * (nu * lmx + atx) + jscale * sF[r];
-    sLy[r * SW + cc] = my + dt * (nu * lmy + aty);
+    sLx[r * SW + cc] = mx + fmaf(cL, lmx, fmaf(cA, atx, jscale * sF[r]));
+    sLy[r * SW + cc] = my + fmaf(cL, lmy, cA * aty);
   });
   __syncthreads();
 
@@ -173,9 +208,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
       lo[g] = sLx[o];
       lo[NN + g] = sLy[o];
-      const float gx = fdiv(fsub(sLx[o + SW], sLx[o - SW]), c.h2);
-      const float gy = fdiv(fsub(sLy[o + 1], sLy[o - 1]), c.h2);
-      rhs[g] = fdiv(fadd(gx, gy), dt);
+      rhs[g] = fused_rhs(sLx[o + SW], sLx[o - SW], sLy[o + 1], sLy[o - 1], c.cD);
     });
   }
 
@@ -205,13 +238,6 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
 }
 
-static size_t adjoint_smem(int tw, int th) {
-  // floats of the tiles and forcing rows, then 24 doubles (8-byte aligned)
-  const size_t f = (size_t)(th + 6) * (tw + 6) + 4 * (size_t)(th + 4) * (tw + 4) +
-                   2 * (size_t)(th + 2) * (tw + 2) + (th + 2) + 2 * th + 2;
-  return f * sizeof(float) + 24 * sizeof(double) + 8;
-}
-
 template <int SCHEME, int TW, int TH>
 static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
   static bool configured = false;
@@ -220,7 +246,7 @@ static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
     configured = true;
   }
   const dim3 grid(a.c.N / TW, a.c.N / TH);
-  k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), adjoint_smem(TW, TH), st>>>(a);
+  k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), AdjointSmem<TW, TH>::BYTES, st>>>(a);
   return cudaGetLastError();
 }
 

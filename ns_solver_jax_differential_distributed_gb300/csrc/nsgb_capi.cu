@@ -922,7 +922,9 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
     const int s0 = seg * every, s1 = std::min(steps, s0 + every);
     const float* rc = g.ckpt + (size_t)seg * 2 * NN;
     const float* rp = nullptr;
-    for (int s = s0; s < s1; ++s) {
+    // a one-step segment's state is its checkpoint: nothing to recompute
+    const bool stored = (s1 - s0 == 1);
+    for (int s = s0; s < s1 && !stored; ++s) {
       float* out = ((s - s0) % 2 == 0) ? w.usA : w.usB;
       NSGB_CUDA(rollout_step(plan, a, rc, rp, out, w, s, nullptr, g.ustore + (size_t)(s - s0) * 2 * NN,
                              s + 1 < s1, st));
@@ -933,7 +935,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
       float* lam_out = (s == 0 && dJdu0) ? dJdu0 : ((lam == g.lamA) ? g.lamB : g.lamA);
       b.lam = lam;
       b.p = have_padj ? g.padj : nullptr;
-      b.u = g.ustore + (size_t)(s - s0) * 2 * NN;
+      b.u = stored ? g.ckpt + (size_t)seg * 2 * NN : g.ustore + (size_t)(s - s0) * 2 * NN;
       b.lam_out = lam_out;
       b.step = s;
       b.gslot = s - s0;

@@ -388,7 +388,7 @@ class SingleCoreNSSolver:
     """
 
     def __init__(self, grid: Grid, phys: Phys, time_cfg: Time, advection_scheme: str = "central",
-                 device=None, checkpoint_every: int = 50, use_graph: bool = True):
+                 device=None, checkpoint_every: Optional[int] = None, use_graph: bool = True):
         self.grid = grid
         self.time = time_cfg
         self.phys = phys
@@ -399,13 +399,26 @@ class SingleCoreNSSolver:
         advection = make_advection_scheme(advection_scheme)
         self.forcing = GaussianForcingField(grid, phys)
         self.projector = ChorinProjector(ops, poisson, advection, phys.nu, time_cfg.dt)
-        self.checkpoint_every = int(checkpoint_every)
+        # None: store every state when they fit in half the free device memory
+        # (no recomputation in the backward pass), else checkpoints every
+        # ceil(sqrt(steps)) steps
+        self.checkpoint_every = None if checkpoint_every is None else int(checkpoint_every)
         self.use_graph = bool(use_graph)
         self._scheme_id = _native.SCHEME_IDS[advection_scheme]
         self.jit_objective = self.objective
         self.jit_gradient = self.gradient_zero_ic
 
     # -- helpers
+    def _every(self) -> int:
+        if self.checkpoint_every is not None:
+            return self.checkpoint_every
+        steps = int(self.time.steps)
+        state = 8 * self.grid.N * self.grid.N
+        free, _ = torch.cuda.mem_get_info(self.device)
+        if (steps + 1) * state <= free // 2:
+            return 1
+        return max(1, math.isqrt(max(steps - 1, 0)) + 1)
+
     def _theta(self, theta) -> torch.Tensor:
         th = _as_f32(theta, self.device).reshape(-1)
         if th.numel() not in (2, 3):
@@ -439,7 +452,7 @@ class SingleCoreNSSolver:
                 (isinstance(u0t, torch.Tensor) and u0t.requires_grad)):
             th_d = th.to(self.device, torch.float32)
             u0_d = u0t.to(self.device, torch.float32)
-            return _RolloutFn.apply(th_d, u0_d, self, self.checkpoint_every)
+            return _RolloutFn.apply(th_d, u0_d, self, self._every())
         th = self._theta(th)
         u0t = self._u(u0t)
         g, ph = self.grid, self.phys
@@ -455,11 +468,11 @@ class SingleCoreNSSolver:
 
     def gradient(self, u0, theta, want_u0_grad: bool = False):
         """dJ/dtheta of rollout(u0, theta) by the discrete adjoint with
-        checkpoints every ``checkpoint_every`` steps.  Returns (J, dJ/dtheta)
-        or (J, dJ/dtheta, dJ/du0)."""
+        checkpoints every ``checkpoint_every`` steps (every state when None
+        and they fit).  Returns (J, dJ/dtheta) or (J, dJ/dtheta, dJ/du0)."""
         g, ph = self.grid, self.phys
         J, gt, _, du0 = _native.rollout_grad_raw(
-            self._u(u0), self._theta(theta), int(self.time.steps), self.checkpoint_every,
+            self._u(u0), self._theta(theta), int(self.time.steps), self._every(),
             float(g.L), float(ph.nu), float(self.time.dt), self._scheme_id, float(ph.mu0),
             float(ph.sigma0), float(ph.C), want_u_final=False, want_du0=want_u0_grad)
         return (J, gt, du0) if want_u0_grad else (J, gt)
