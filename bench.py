@@ -52,9 +52,10 @@ def parse_args(argv=None):
     ap.add_argument("--scheme", choices=["central", "upwind"], default="central")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["plain", "grad", "ensemble", "serve"], default="plain",
+    ap.add_argument("--workload", choices=["plain", "grad", "ensemble", "serve", "optimize"], default="plain",
                     help="plain: the headline N=4096 rollout (default); grad: N=1024 adjoint; "
-                         "ensemble: 256 uneven solves; serve: Poisson-arrival serving")
+                         "ensemble: 256 uneven solves; serve: Poisson-arrival serving; optimize: the "
+                         "reference's optimiser study on the device")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
     return ap.parse_args(argv)
@@ -422,6 +423,48 @@ def run_grad(args):
             "dtype": "f32", "data": "synthetic"}
 
 
+def run_optimize(args):
+    """The reference's parameter optimisation study (studies.py:864-934):
+    Adam (lr 0.01, 0.001), SGD (lr 0.1), RMSprop (lr 0.01), 100 steps each
+    from theta0 = [1, 0.5], objective from the zero state at N=128, L=1,
+    nu=0.01, 328 steps (SimConfig's dt), central -- each optimiser one
+    nsgb_optimize call.  Reports device time per optimiser step (one adjoint
+    gradient + update) and the final objectives; the reference's CPU run of
+    the same study takes 0.119 s per jit_gradient call (BASELINE)."""
+    import torch
+    import ns_solver_jax_differential_distributed_gb300 as nsgb
+    from ns_solver_jax_differential_distributed_gb300 import _build, autotune, optimization
+    _build.build()
+    dev = torch.device("cuda", 0)
+    N, L, nu, steps = 128, 1.0, 0.01, 328
+    dt = float(np.float32(min(0.4 * (L / N), (L / N) ** 2 / (4 * nu))))
+    autotune.tune(N, L, "central", dev)
+    solver = nsgb.SingleCoreNSSolver(nsgb.make_grid(N, L), nsgb.Phys(nu=nu, mu0=0.5, sigma0=0.1, C=1.0),
+                                     nsgb.Time(dt=dt, steps=steps), "central", device=dev)
+    study = optimization.ParameterOptimizationStudy(solver.jit_objective, solver.jit_gradient, [1.0, 0.5],
+                                                    optim_steps=100)
+    study.run_all()  # warm-up (plans, workspaces)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record()
+    res = study.run_all()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    n_steps = 4 * 100
+    return {"metric": "optimiser steps/s", "value": n_steps / (e0.elapsed_time(e1) / 1e3), "unit": "steps/s",
+            "higher_is_better": True, "ms_per_optimizer_step": e0.elapsed_time(e1) / n_steps,
+            "wall_s": wall, "config": {"N": N, "L": L, "nu": nu, "dt": dt, "steps": steps, "scheme": "central",
+                                       "theta0": [1.0, 0.5], "optim_steps": 100,
+                                       "checkpoint_every": solver._every()},
+            "final": {k: {"obj_initial": v["obj_initial"], "obj_final": v["obj_final"],
+                          "improvement": v["improvement"],
+                          "theta_final": np.asarray(v["history"]["parameters"][-1]).tolist()}
+                      for k, v in res.items()},
+            "reference_cpu_s_per_gradient": 0.119, "dtype": "f32", "data": "synthetic"}
+
+
 def run_ensemble(args):
     """Batching: 256 solves, N in {64,128,256,512} w.p. {.4,.3,.2,.1}, 500
     steps, per-solve nu/theta/u0; one batched launch per stage per N-group,
@@ -495,7 +538,8 @@ def main(argv=None):
     world, rank, local = dist_env()
     if args.workload != "plain":
         if rank == 0:
-            fn = {"grad": run_grad, "ensemble": run_ensemble, "serve": run_serve}[args.workload]
+            fn = {"grad": run_grad, "ensemble": run_ensemble, "serve": run_serve,
+                  "optimize": run_optimize}[args.workload]
             print(json.dumps(fn(args)), flush=True)
         return
     if args.impl == "reference":

@@ -218,6 +218,39 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
                      size_t flush_bytes, void* workspace, size_t workspace_bytes, float* out_ms,
                      void* stream);
 
+/* Optimisers of ParameterOptimizationStudy (studies.py:879-884): optax
+ * 0.2.4's sgd, adam and rmsprop, whose update rules nsgb_optim.cu restates. */
+#define NSGB_OPT_SGD 0
+#define NSGB_OPT_ADAM 1
+#define NSGB_OPT_RMSPROP 2
+
+typedef struct nsgb_optimizer {
+  int kind;             /* NSGB_OPT_* */
+  double learning_rate;
+  double b1, b2;        /* adam moment decays (optax defaults 0.9, 0.999) */
+  double eps;           /* adam: added to sqrt(v_hat); rmsprop: inside the sqrt (1e-8) */
+  double eps_root;      /* adam: inside the sqrt (0) */
+  double decay;         /* rmsprop second-moment decay (0.9) */
+} nsgb_optimizer;
+
+/* Workspace of nsgb_optimize: the gradient workspace of (steps, every) plus
+ * the parameters, gradient, optimiser moments and two state fields.  0 on an
+ * invalid argument. */
+size_t nsgb_optimize_workspace_bytes(const nsgb_plan* plan, int steps, int every, int theta_len);
+
+/* ParameterOptimizationStudy._run_single_optimizer (studies.py:890-934) on
+ * the device: from theta0, `iters` optimiser steps theta_{k+1} = theta_k +
+ * update(dJ/dtheta(theta_k)), the gradient by the discrete adjoint of a
+ * `steps`-step rollout (nsgb_rollout_grad, checkpoints every `every` steps)
+ * from u0, or from the zero state when u0 is NULL (objective / jit_gradient,
+ * NS_solver.py:724-725, 752-756).  Writes objectives[k] = J(theta_k) for
+ * k = 0..iters and parameters[k * theta_len ...] = theta_k (device arrays of
+ * iters + 1 and (iters + 1) * theta_len floats).  Every launch is ordered on
+ * `stream`; the host never waits.  theta_len 2 ([A, B]) or 3 ([A, B, nu]). */
+int nsgb_optimize(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta0,
+                  int theta_len, int steps, int every, const nsgb_optimizer* opt, int iters, float* objectives,
+                  float* parameters, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Largest N accepted by nsgb_poisson_noalloc. */
 #define NSGB_NOALLOC_MAX_N 1024
 

@@ -39,6 +39,16 @@ class Member(ctypes.Structure):
                 ("done_steps", ctypes.c_int)]
 
 
+class Optimizer(ctypes.Structure):
+    """``nsgb_optimizer`` (include/nsgb.h)."""
+    _fields_ = [("kind", ctypes.c_int), ("learning_rate", ctypes.c_double), ("b1", ctypes.c_double),
+                ("b2", ctypes.c_double), ("eps", ctypes.c_double), ("eps_root", ctypes.c_double),
+                ("decay", ctypes.c_double)]
+
+
+OPT_SGD, OPT_ADAM, OPT_RMSPROP = 0, 1, 2
+
+
 class NativeError(RuntimeError):
     """A C-ABI call returned a non-zero status."""
 
@@ -82,6 +92,8 @@ SIGNATURES = {
     "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_poisson_noalloc": ([_I, _D, _P, _P, _P], _I),
+    "nsgb_optimize_workspace_bytes": ([_P, _I, _I, _I], _S),
+    "nsgb_optimize": ([_P, _PH, _P, _P, _I, _I, _I, ctypes.POINTER(Optimizer), _I, _P, _P, _P, _S, _P], _I),
 }
 
 
@@ -428,3 +440,29 @@ def time_stages(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: 
          ptr(flush), 0 if flush is None else flush.numel() * flush.element_size(), ptr(ws), ws.numel(),
          out, st)
     return dict(zip(STAGES, list(out)))
+
+
+def optimize(theta0: torch.Tensor, steps: int, every: int, N: int, L: float, nu: float, dt: float, scheme,
+             opt: Optimizer, iters: int, u0: torch.Tensor | None = None, mu0=0.5, sigma0=0.1, C=1.0):
+    """nsgb_optimize: `iters` optimiser steps on the device from theta0 (zero
+    initial state when u0 is None).  Returns (objectives[iters+1],
+    parameters[iters+1, len(theta0)]) as device tensors."""
+    theta0 = _cuda_f32(theta0, "theta0")
+    dev = theta0.device
+    if u0 is not None:
+        u0 = _cuda_f32(u0, "u0")
+        if _square(u0, "u0", 2) != N:
+            raise ValueError(f"u0 must be (2, {N}, {N})")
+    p = get_plan(N, L, dev)
+    st = stream_of(dev)
+    ph = make_phys(L, nu, dt, scheme, mu0, sigma0, C)
+    n = theta0.numel()
+    nbytes = lib().nsgb_optimize_workspace_bytes(p.handle, int(steps), int(every), n)
+    if nbytes == 0:
+        raise ValueError("invalid optimisation arguments (steps >= 1, every >= 1, theta of 2 or 3 entries)")
+    ws = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    objectives = torch.empty(iters + 1, dtype=torch.float32, device=dev)
+    parameters = torch.empty(iters + 1, n, dtype=torch.float32, device=dev)
+    call("nsgb_optimize", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta0), n, int(steps), int(every),
+         ctypes.byref(opt), int(iters), ptr(objectives), ptr(parameters), ptr(ws), ws.numel(), st)
+    return objectives, parameters

@@ -952,6 +952,99 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   return NSGB_OK;
 }
 
+// ----------------------------------------------------------- optimiser --
+namespace {
+struct OptWs {
+  GradWs g;
+  float *theta, *grad, *mu, *nu, *zero_u, *u_final;
+  size_t bytes;
+};
+
+OptWs carve_opt(const nsgb_plan* plan, int steps, int every, void* ws) {
+  const size_t NN = (size_t)plan->N * plan->N;
+  OptWs o;
+  o.g = carve_grad(plan, steps, every, ws);
+  Carver cv(ws);
+  cv.off = o.g.bytes;
+  o.theta = cv.take<float>(4);
+  o.grad = cv.take<float>(4);
+  o.mu = cv.take<float>(4);
+  o.nu = cv.take<float>(4);
+  o.zero_u = cv.take<float>(2 * NN);
+  o.u_final = cv.take<float>(2 * NN);
+  o.bytes = cv.off;
+  return o;
+}
+
+OptimizerRule optimizer_rule(const nsgb_optimizer& o, int count) {
+  OptimizerRule r{};
+  r.kind = o.kind;
+  r.lr = (float)o.learning_rate;
+  r.b1 = (float)o.b1;
+  r.b2 = (float)o.b2;
+  r.one_minus_b1 = (float)(1.0 - o.b1);
+  r.one_minus_b2 = (float)(1.0 - o.b2);
+  r.bc1 = (float)(1.0 - std::pow(o.b1, (double)count));
+  r.bc2 = (float)(1.0 - std::pow(o.b2, (double)count));
+  r.eps = (float)o.eps;
+  r.eps_root = (float)o.eps_root;
+  r.decay = (float)o.decay;
+  r.one_minus_decay = (float)(1.0 - o.decay);
+  return r;
+}
+}  // namespace
+
+size_t nsgb_optimize_workspace_bytes(const nsgb_plan* plan, int steps, int every, int theta_len) {
+  if (!plan || steps < 1 || every < 1 || (theta_len != 2 && theta_len != 3)) return 0;
+  return carve_opt(plan, steps, every, nullptr).bytes;
+}
+
+int nsgb_optimize(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta0,
+                  int theta_len, int steps, int every, const nsgb_optimizer* opt, int iters, float* objectives,
+                  float* parameters, void* workspace, size_t ws_bytes, void* stream) {
+  if (int r = check_plan(plan)) return r;
+  if (int r = check_phys(phys)) return r;
+  if (int r = check_theta(theta0, theta_len)) return r;
+  if (u0)
+    if (int r = check_field(u0, "u0")) return r;
+  if (!opt) return fail(NSGB_ERR_INVALID_ARG, "optimizer is NULL");
+  if (opt->kind != NSGB_OPT_SGD && opt->kind != NSGB_OPT_ADAM && opt->kind != NSGB_OPT_RMSPROP)
+    return fail(NSGB_ERR_INVALID_ARG, "unknown optimizer kind %d", opt->kind);
+  if (!(std::isfinite(opt->learning_rate) && std::isfinite(opt->b1) && std::isfinite(opt->b2) &&
+        std::isfinite(opt->eps) && std::isfinite(opt->eps_root) && std::isfinite(opt->decay)))
+    return fail(NSGB_ERR_INVALID_ARG, "optimizer hyper-parameters must be finite");
+  if (steps < 1) return fail(NSGB_ERR_INVALID_ARG, "steps must be >= 1");
+  if (every < 1) return fail(NSGB_ERR_INVALID_ARG, "checkpoint interval must be >= 1");
+  if (iters < 0) return fail(NSGB_ERR_INVALID_ARG, "iters must be >= 0");
+  if (!objectives || !parameters) return fail(NSGB_ERR_INVALID_ARG, "NULL history pointer");
+  const size_t need = carve_opt(plan, steps, every, nullptr).bytes;
+  if (int r = check_ws(workspace, ws_bytes, need)) return r;
+  OptWs o = carve_opt(plan, steps, every, workspace);
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t NN = (size_t)plan->N * plan->N;
+  const size_t tb = (size_t)theta_len * sizeof(float);
+  NSGB_CUDA(cudaMemcpyAsync(o.theta, theta0, tb, cudaMemcpyDeviceToDevice, st));
+  NSGB_CUDA(cudaMemcpyAsync(parameters, theta0, tb, cudaMemcpyDeviceToDevice, st));
+  NSGB_CUDA(cudaMemsetAsync(o.mu, 0, 4 * sizeof(float), st));
+  NSGB_CUDA(cudaMemsetAsync(o.nu, 0, 4 * sizeof(float), st));
+  if (!u0) {
+    NSGB_CUDA(cudaMemsetAsync(o.zero_u, 0, 2 * NN * sizeof(float), st));
+    u0 = o.zero_u;
+  }
+  const size_t grad_bytes = o.g.bytes;
+  for (int k = 0; k < iters; ++k) {
+    if (int r = nsgb_rollout_grad(plan, phys, u0, o.theta, theta_len, steps, every,
+                                  NSGB_GRAD_FORWARD | NSGB_GRAD_BACKWARD, objectives + k, nullptr, o.grad,
+                                  nullptr, workspace, grad_bytes, stream))
+      return r;
+    NSGB_CUDA(launch_optimizer_update(optimizer_rule(*opt, k + 1), k + 1, o.theta, o.grad, o.mu, o.nu,
+                                      parameters + (size_t)(k + 1) * theta_len, theta_len, st));
+  }
+  // objective at the last parameters (the study evaluates it after each update)
+  return nsgb_rollout(plan, phys, u0, o.theta, theta_len, steps, o.u_final, objectives + iters, workspace,
+                      grad_bytes, 0, stream);
+}
+
 size_t nsgb_ensemble_workspace_bytes(const nsgb_member* members, int count) {
   if (!members || count <= 0) return 0;
   for (int i = 0; i < count; ++i)

@@ -128,6 +128,16 @@ cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
 cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
 cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st);
 
+// ------------------------------------------------------------- optimiser --
+// Constants of one optimiser update, float32 as the library rounds them;
+// bc1/bc2 = 1 - b^t for the step count t of the launch.
+struct OptimizerRule {
+  int kind;
+  float lr, b1, b2, one_minus_b1, one_minus_b2, bc1, bc2, eps, eps_root, decay, one_minus_decay;
+};
+cudaError_t launch_optimizer_update(const OptimizerRule& r, int count, float* theta, const float* grad, float* mu,
+                                    float* nu, float* theta_copy, int n, cudaStream_t st);
+
 // Record the message nsgb_last_error() returns on this host thread.
 void set_last_error(const char* msg);
 

@@ -8,8 +8,9 @@ reads them from a reference checkout and writes small fixtures next to itself:
 * ``reference_results.json`` -- objectives / kinetic energies / max speeds of the
   viscosity and scheme studies (studies.py:118-167, 552-601), the SGD(lr=0.1)
   trajectory of the optimisation study (studies.py:890-934), from which the JAX
-  reverse-mode gradient follows as (theta_k - theta_{k+1}) / 0.1, and the
-  configurations each number was produced with;
+  reverse-mode gradient follows as (theta_k - theta_{k+1}) / 0.1, the
+  trajectories of all four optimisers of that study, and the configurations
+  each number was produced with;
 * ``speed_single_N128.npy`` -- |u| after runner.py's single-device run at
   N=128 (runner.py:115-175, sample_config/config_N_128.json);
 * ``speed_P8_N512_sub4.npy`` -- every 4th point (both axes) of |u| after the
@@ -78,6 +79,17 @@ def main(ref: str) -> None:
         base, nu=0.01, scheme="central", dt=dt, steps=simconfig_steps(0.5, dt), lr=0.1,
         parameters=opt["SGD (lr=0.1)_parameters"].astype(np.float64).tolist(),
         objectives=opt["SGD (lr=0.1)_objectives"].astype(np.float64).tolist())
+    # All four optimiser trajectories of ParameterOptimizationStudy
+    # (studies.py:879-884, optax 0.2.4 defaults), 100 steps from theta0.
+    runs = []
+    for name in ("Adam (lr=0.01)", "Adam (lr=0.001)", "SGD (lr=0.1)", "RMSprop (lr=0.01)"):
+        runs.append(dict(name=name, obj_initial=float(opt[f"{name}_obj_initial"]),
+                         obj_final=float(opt[f"{name}_obj_final"]),
+                         improvement=float(opt[f"{name}_improvement"]),
+                         parameters=opt[f"{name}_parameters"].astype(np.float64).tolist(),
+                         objectives=opt[f"{name}_objectives"].astype(np.float64).tolist()))
+    out["studies"]["optimizers"] = dict(base, nu=0.01, scheme="central", dt=dt,
+                                        steps=simconfig_steps(0.5, dt), optim_steps=100, runs=runs)
 
     # Speed fields of runner.py (sample configs: nu=1e-4, t=0.5, central, L=1).
     s128 = np.load(os.path.join(res, "velocity_magnitude_single_N128.npy")).astype(np.float32)
