@@ -54,6 +54,77 @@ def benchmark_callable(label: str, fn: Callable, *args, warmup: int = 1, runs: i
     return ProfileSummary(label, float(a.mean()), float(a.min()), float(a.max()), float(a.std()))
 
 
+class SolverKernelProfiler:
+    """Stage profiling of the single-core solver (solver_profiler.py:23-240,
+    whose distributed half is out of scope): forcing, advection_diffusion,
+    pressure_solve and projection through the solver's own strategy objects
+    (each stage one or a few kernels of libnsgb), then the fused full step and
+    the full rollout."""
+
+    def __init__(self, logger=None):
+        import logging
+        self.logger = logger if logger is not None else logging.getLogger(__name__)
+
+    @classmethod
+    def benchmark_callable(cls, label: str, fn: Callable, *args, warmup: int = 1, runs: int = 5) -> ProfileSummary:
+        return benchmark_callable(label, fn, *args, warmup=warmup, runs=runs)
+
+    def _log_profile_table(self, title: str, rows: List[ProfileSummary]) -> None:
+        self.logger.info("-" * 80)
+        self.logger.info(title)
+        self.logger.info("-" * 80)
+        self.logger.info(f"{'Kernel':36s} {'mean [s]':>12s} {'min [s]':>12s} {'max [s]':>12s} {'std [s]':>12s}")
+        for row in rows:
+            self.logger.info(f"{row.label:36s} {row.mean_sec:12.6f} {row.min_sec:12.6f} {row.max_sec:12.6f} "
+                             f"{row.std_sec:12.6f}")
+
+    def profile_solver_kernels(self, single, theta, warmup: int = 1, runs: int = 5) -> List[ProfileSummary]:
+        import torch
+        dev = single.device
+        N, dt = single.grid.N, single.time.dt
+        pr = single.projector
+        ops, adv, poi, nu = pr.ops, pr.advection, pr.poisson, pr.nu
+        theta = torch.as_tensor(theta, dtype=torch.float32).to(dev)
+        u0 = torch.zeros((2, N, N), dtype=torch.float32, device=dev)
+        t0 = 0.0
+
+        def s_forcing(th, t):
+            return single.forcing(th, t)
+
+        def s_advec_diff(u, f):
+            ux, uy = u[0], u[1]
+            ux_s = ux + dt * (nu * ops.laplacian(ux) + adv.advect(ux, ux, uy, ops) + f[0])
+            uy_s = uy + dt * (nu * ops.laplacian(uy) + adv.advect(uy, ux, uy, ops) + f[1])
+            return torch.stack([ux_s, uy_s])
+
+        def s_pressure(us):
+            return poi(ops.divergence(us) / dt)
+
+        def s_projection(us, p):
+            px, py = ops.grad(p)
+            return torch.stack([us[0] - dt * px, us[1] - dt * py])
+
+        f = s_forcing(theta, t0)
+        us = s_advec_diff(u0, f)
+        p = s_pressure(us)
+        rows = [
+            self.benchmark_callable("single: forcing", s_forcing, theta, t0, warmup=warmup, runs=runs),
+            self.benchmark_callable("single: advection_diffusion", s_advec_diff, u0, f, warmup=warmup, runs=runs),
+            self.benchmark_callable("single: pressure_solve", s_pressure, us, warmup=warmup, runs=runs),
+            self.benchmark_callable("single: projection", s_projection, us, p, warmup=warmup, runs=runs),
+            self.benchmark_callable("single: full_step", single.step, u0, theta, t0, warmup=warmup, runs=runs),
+            self.benchmark_callable("single: full_rollout", single.rollout, u0, theta, warmup=warmup,
+                                    runs=max(1, min(runs, 3))),
+        ]
+        self._log_profile_table("Single-core solver stages", rows)
+        return rows
+
+
+def profile_solver_kernels(single_solver, theta, warmup: int = 1, runs: int = 5, logger=None):
+    """solver_profiler.py's entry point for the single-core solver."""
+    return SolverKernelProfiler(logger).profile_solver_kernels(single_solver, theta, warmup=warmup, runs=runs)
+
+
 def main(argv=None):
     import torch
     from . import _build, _native

@@ -9,8 +9,9 @@ reads them from a reference checkout and writes small fixtures next to itself:
   viscosity and scheme studies (studies.py:118-167, 552-601), the SGD(lr=0.1)
   trajectory of the optimisation study (studies.py:890-934), from which the JAX
   reverse-mode gradient follows as (theta_k - theta_{k+1}) / 0.1, the
-  trajectories of all four optimisers of that study, and the configurations
-  each number was produced with;
+  trajectories of all four optimisers of that study, the finite-difference
+  error sweep of the gradient benchmark (studies.py:271-521), and the
+  configurations each number was produced with;
 * ``speed_single_N128.npy`` -- |u| after runner.py's single-device run at
   N=128 (runner.py:115-175, sample_config/config_N_128.json);
 * ``speed_P8_N512_sub4.npy`` -- every 4th point (both axes) of |u| after the
@@ -90,6 +91,16 @@ def main(ref: str) -> None:
                          objectives=opt[f"{name}_objectives"].astype(np.float64).tolist()))
     out["studies"]["optimizers"] = dict(base, nu=0.01, scheme="central", dt=dt,
                                         steps=simconfig_steps(0.5, dt), optim_steps=100, runs=runs)
+
+    # GradientBenchmark (studies.py:271-521): central-FD vs JAX gradient over
+    # 20 step sizes for three parameter vectors, config of the optimiser study.
+    gb = np.load(os.path.join(res, "gradient_benchmark_results.npz"))
+    out["studies"]["gradient_benchmark"] = dict(
+        base, nu=0.01, scheme="central", dt=dt, steps=simconfig_steps(0.5, dt),
+        param_vectors=[[1.0, 0.5], [0.5, 0.5], [2.0, 1.0]],  # studies.py:1064-1074
+        epsilons=gb["param_0_epsilons"].astype(np.float64).tolist(),
+        rel_errors=[gb[f"param_{i}_rel_errors"].astype(np.float64).tolist() for i in range(3)],
+        time_jax_exec_mean=[float(gb[f"param_{i}_time_jax_exec_mean"]) for i in range(3)])
 
     # Speed fields of runner.py (sample configs: nu=1e-4, t=0.5, central, L=1).
     s128 = np.load(os.path.join(res, "velocity_magnitude_single_N128.npy")).astype(np.float32)

@@ -137,3 +137,22 @@ def test_full_size_N4096(nsgb, scheme):
     div = (torch.roll(ua[0], -1, 0) - torch.roll(ua[0], 1, 0) + torch.roll(ua[1], -1, 1)
            - torch.roll(ua[1], 1, 1)) / (2 * dx)
     assert float(div.abs().max()) < 1e-2 * float(ua.abs().max()) / dx
+
+
+def test_runner_writes_reference_speed_field(nsgb, golden, tmp_path, monkeypatch):
+    """runner.main with the reference's sample config for N=128 writes the
+    reference's output file, whose content matches the speed field the
+    reference shipped (runner.py:162-175); --profile times the stages."""
+    import json
+    import os
+    from ns_solver_jax_differential_distributed_gb300 import runner
+    f = golden["speed_fields"][0]
+    ref = np.load(os.path.join(os.path.dirname(__file__), "golden", f["file"]))
+    cfg = tmp_path / "config_N_128.json"
+    cfg.write_text(json.dumps({"N": 128, "nu": 0.0001, "t": 0.5, "advection_scheme": "central"}))
+    monkeypatch.chdir(tmp_path)
+    out = runner.main(["--config", str(cfg), "--profile", "--profile-warmup", "1", "--profile-runs", "2"])
+    assert out["path"] == "result/velocity_magnitude_single_N128.npy"
+    speed = np.load(tmp_path / out["path"])
+    assert speed.shape == (128, 128) and speed.dtype == np.float32
+    assert rel_l2(ref, speed.astype(np.float64)) < 1e-6
