@@ -152,7 +152,36 @@ __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, in
     float2 x[RP];
 #pragma unroll
     for (int r = 0; r < RP; ++r) x[r] = a[q + r * Q];
-    if constexpr (NS > 1) {
+    if constexpr (NS > 1 && RP == 16) {
+      // W^r for r = 1..15 from the table's W^1, W^2, W^4, W^8 and at most two
+      // complex products each (a few ulps), so a radix-16 pass issues 4
+      // twiddle loads instead of 15
+      const int bm = b & (NS - 1);
+      const float2* __restrict__ tp = tw + tw_offset<E>(NS) + bm;
+      float2 w1 = __ldg(tp + NS), w2 = __ldg(tp + 2 * NS), w4 = __ldg(tp + 4 * NS), w8 = __ldg(tp + 8 * NS);
+      if (INV) {
+        w1.y = -w1.y;
+        w2.y = -w2.y;
+        w4.y = -w4.y;
+        w8.y = -w8.y;
+      }
+      const float2 w3 = cmul(w2, w1), w12 = cmul(w8, w4);
+      x[1] = cmul(x[1], w1);
+      x[2] = cmul(x[2], w2);
+      x[3] = cmul(x[3], w3);
+      x[4] = cmul(x[4], w4);
+      x[5] = cmul(x[5], cmul(w4, w1));
+      x[6] = cmul(x[6], cmul(w4, w2));
+      x[7] = cmul(x[7], cmul(w4, w3));
+      x[8] = cmul(x[8], w8);
+      x[9] = cmul(x[9], cmul(w8, w1));
+      x[10] = cmul(x[10], cmul(w8, w2));
+      x[11] = cmul(x[11], cmul(w8, w3));
+      x[12] = cmul(x[12], w12);
+      x[13] = cmul(x[13], cmul(w12, w1));
+      x[14] = cmul(x[14], cmul(w12, w2));
+      x[15] = cmul(x[15], cmul(w12, w3));
+    } else if constexpr (NS > 1) {
       const int bm = b & (NS - 1);
       const float2* __restrict__ tp = tw + tw_offset<E>(NS) + bm;
 #pragma unroll
