@@ -75,11 +75,58 @@ class Ensemble:
             arr[k].total_steps = self.steps
             arr[k].done_steps = 0
         self._members = arr
-        L = _bind()
-        nbytes = L.nsgb_ensemble_workspace_bytes(arr, len(self.specs))
+        self.workspace = torch.empty(0, dtype=torch.uint8, device=self.device)
+        self._ensure_workspace()
+        if tune:
+            self.tune_batched()
+
+    def _ensure_workspace(self) -> None:
+        """Size the workspace for the plans' current launch shapes."""
+        nbytes = _bind().nsgb_ensemble_workspace_bytes(self._members, len(self.specs))
         if nbytes == 0:
             raise ValueError("invalid ensemble")
-        self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        if self.workspace.numel() < nbytes:
+            self.workspace = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+
+    def _time_run(self) -> float:
+        self.run()
+        torch.cuda.synchronize(self.device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        self.run()
+        e1.record()
+        torch.cuda.synchronize(self.device)
+        return e0.elapsed_time(e1)
+
+    def tune_batched(self) -> None:
+        """Choose each grid size's stencil shape for batched launches by timing
+        the whole ensemble: the single-solve tuner favours short row bands
+        (one solve must fill the GPU), while a batch gets its parallelism from
+        its members and prefers taller bands, whose halo overhead is smaller.
+        Largest groups first; FFT shapes stay as tuned for single solves."""
+        cells = {}
+        for s in self.specs:
+            cells[(s.N, s.L)] = cells.get((s.N, s.L), 0) + s.N * s.N
+        for (N, L) in sorted(cells, key=cells.get, reverse=True):
+            plan = _native.get_plan(N, L, self.device)
+            base = plan.tiles()
+            cands = [tuple(base[:2])]
+            if N >= 64:
+                cands += [(64, 16), (128, 8)] if N >= 128 else [(64, 16)]
+            if N >= 128:
+                cands += [(max(256, min(512, N)), h) for h in (16, 32) if h <= N]
+            best, best_ms = tuple(base[:2]), None
+            for (tw, th) in dict.fromkeys(cands):
+                try:
+                    plan.set_tiles(tw, th, base[2], base[3])
+                except _native.NativeError:
+                    continue
+                self._ensure_workspace()
+                ms = self._time_run()
+                if best_ms is None or ms < best_ms:
+                    best, best_ms = (tw, th), ms
+            plan.set_tiles(best[0], best[1], base[2], base[3])
+            self._ensure_workspace()
 
     @property
     def cell_steps(self) -> int:
@@ -87,6 +134,7 @@ class Ensemble:
 
     def run(self):
         """Advance every member; returns (J[count], [u_final...])."""
+        self._ensure_workspace()
         L = _bind()
         _native.check("nsgb_ensemble_rollout", L.nsgb_ensemble_rollout(
             self._members, len(self.specs), self.chunk, self.workspace.data_ptr(),
@@ -96,6 +144,7 @@ class Ensemble:
     def run_advance(self, steps_per_call: int):
         """The same ensemble through nsgb_ensemble_advance in slices of
         ``steps_per_call`` steps (the continuous-batching entry point)."""
+        self._ensure_workspace()
         L = _bind()
         done = 0
         while True:
