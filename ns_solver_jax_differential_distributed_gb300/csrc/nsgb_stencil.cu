@@ -234,9 +234,17 @@ inline size_t smem_bytes(int N, int W, int RH) {
   return sizeof(float) * ((size_t)(kPRing + 2 * kURing) * ring_stride(W) + (size_t)12 * groups(N, W) + RH + 2 + 32);
 }
 
-__device__ __forceinline__ void cp16(float* dst_smem, const float* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
-               "l"(src)
+// Input rows are read once: their copies carry an L2 evict-first policy, so
+// they do not push the FFT passes' fields out of L2.
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ void cp16(float* dst_smem, const float* src, uint64_t pol) {
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(dst_smem)),
+               "l"(src), "l"(pol)
                : "memory");
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
@@ -247,6 +255,11 @@ __device__ __forceinline__ void cp_wait() {
 
 __device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
   *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
+}
+// Evict-first store, for u*next: it is read only by the next step's stencil,
+// after the FFT passes, so it should not push their inputs out of L2.
+__device__ __forceinline__ void st4_stream(float* __restrict__ base, size_t off, const float (&v)[4]) {
+  __stcs(reinterpret_cast<float4*>(base + off), make_float4(v[0], v[1], v[2], v[3]));
 }
 __device__ __forceinline__ void ld4s(const float* s, float (&o)[4]) {
   const float4 v = *reinterpret_cast<const float4*>(s);
@@ -303,20 +316,21 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   const float* __restrict__ pp = a.p;
   const float* __restrict__ usx_g = a.us;
   const float* __restrict__ usy_g = a.us + NN;
-  // one copy group: p row `pr` (pr > -1000) and u* row `ur` (ur > -1000)
+  // one copy group: p row `pr` (if do_p) and u* row `ur` (if do_u)
+  const uint64_t pol = evict_first_policy();
   auto issue = [=](int pr, bool do_p, int ur, bool do_u) {
     if (do_p && has_p) {
       float* dst = sP + (pr & (kPRing - 1)) * RS;
       const float* src = pp + (size_t)(pr & M) * N;
-      if (active) cp16(dst + bi, src + col);
-      if (wrap && tid == 0) cp16(dst + 4, src + N - 4);
-      if (wrap && tid == G - 1) cp16(dst + N + 8, src);
+      if (active) cp16(dst + bi, src + col, pol);
+      if (wrap && tid == 0) cp16(dst + 4, src + N - 4, pol);
+      if (wrap && tid == G - 1) cp16(dst + N + 8, src, pol);
     }
     if (do_u && active) {
       const int slot = (ur & (kURing - 1)) * RS + bi;
       const size_t o = (size_t)(ur & M) * N + col;
-      cp16(sUX + slot, usx_g + o);
-      cp16(sUY + slot, usy_g + o);
+      cp16(sUX + slot, usx_g + o, pol);
+      cp16(sUY + slot, usy_g + o, pol);
     }
     cp_commit();
   };
@@ -385,8 +399,8 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       for (int k = 0; k < 4; ++k) rh[k] = fused_rhs(sx1[k], sx3[k], Y2[k + 2], Y2[k], c.cD);
       if (store) {
         const size_t o = (size_t)((t - 2) & M) * N + col;
-        st4(uso_x, o, sx2);
-        st4(uso_y, o, sy2);
+        st4_stream(uso_x, o, sx2);
+        st4_stream(uso_y, o, sy2);
         st4(rhs_g, o, rh);
         if (a.u_out) {
           st4(a.u_out, o, u2x);
