@@ -240,11 +240,8 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
 
 template <int SCHEME, int TW, int TH>
 static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_adjoint<SCHEME, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    configured = true;
-  }
+  const cudaError_t e = raise_smem_limit(k_adjoint<SCHEME, TW, TH>);
+  if (e != cudaSuccess) return e;
   const dim3 grid(a.c.N / TW, a.c.N / TH);
   k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), AdjointSmem<TW, TH>::BYTES, st>>>(a);
   return cudaGetLastError();

@@ -507,6 +507,26 @@ cudaError_t rollout_step(const nsgb_plan* plan, StencilArgs a, const float* us_i
 
 void nsgb::set_last_error(const char* msg) { g_last_error = msg; }
 
+cudaError_t nsgb::raise_smem_limit(const void* kernel) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, cudaError_t> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(kernel, dev);
+  const auto it = done.find(key);
+  if (it != done.end()) return it->second;
+  int optin = 0;
+  cudaFuncAttributes fa;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kernel);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+  if (e == cudaSuccess) done[key] = e;  // failures are retried on the next launch
+  return e;
+}
+
 // ============================================================== C ABI ====
 extern "C" {
 

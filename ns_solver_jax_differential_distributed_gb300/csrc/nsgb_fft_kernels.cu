@@ -229,21 +229,15 @@ static const float2* radix_tables(const FftLaunch& L) {
   return L.tw + (E == 8 ? fft::tw8_offset(N) : 0);
 }
 
-template <class K>
-static void allow_smem(K kernel) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-}
 
 template <int N, int E>
 static cudaError_t stage_rows_fwd(const FftLaunch& L, const SolveDev* sv, int count, cudaStream_t st) {
   constexpr int T = N / E;
   const int P = L.rows_per_cta / 2;
   const size_t smem = (size_t)P * pair_stride<N>() * sizeof(float2);
-  static bool configured = false;  // per-process attribute set-up (idempotent)
-  if (!configured) {
-    allow_smem(k_rows_fwd<N, E>);
-    allow_smem(k_rows_fwd_b<N, E>);
-    configured = true;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = raise_smem_limit(sv ? (const void*)k_rows_fwd_b<N, E> : (const void*)k_rows_fwd<N, E>);
+    if (e != cudaSuccess) return e;
   }
   if (sv)
     k_rows_fwd_b<N, E><<<dim3(N / (2 * P), count), dim3(T, P), smem, st>>>(sv, radix_tables<N, E>(L));
@@ -257,11 +251,9 @@ static cudaError_t stage_cols(const FftLaunch& L, const SolveDev* sv, int count,
   constexpr int T = N / E;
   const int KB = L.cols_per_cta;
   const size_t smem = (size_t)KB * pair_stride<N>() * sizeof(float2);
-  static bool configured = false;
-  if (!configured) {
-    allow_smem(k_cols<N, E>);
-    allow_smem(k_cols_b<N, E>);
-    configured = true;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = raise_smem_limit(sv ? (const void*)k_cols_b<N, E> : (const void*)k_cols<N, E>);
+    if (e != cudaSuccess) return e;
   }
   if (sv)
     k_cols_b<N, E><<<dim3((N / 2) / KB + 1, count), dim3(T, KB), smem, st>>>(sv, radix_tables<N, E>(L), L.k2,
@@ -276,11 +268,9 @@ static cudaError_t stage_rows_inv(const FftLaunch& L, const SolveDev* sv, int co
   constexpr int T = N / E;
   const int P = L.rows_per_cta / 2;
   const size_t smem = (size_t)P * pair_stride<N>() * sizeof(float2);
-  static bool configured = false;
-  if (!configured) {
-    allow_smem(k_rows_inv<N, E>);
-    allow_smem(k_rows_inv_b<N, E>);
-    configured = true;
+  if (smem > 48 * 1024) {
+    const cudaError_t e = raise_smem_limit(sv ? (const void*)k_rows_inv_b<N, E> : (const void*)k_rows_inv<N, E>);
+    if (e != cudaSuccess) return e;
   }
   if (sv)
     k_rows_inv_b<N, E><<<dim3(N / (2 * P), count), dim3(T, P), smem, st>>>(sv, radix_tables<N, E>(L));

@@ -141,4 +141,15 @@ cudaError_t launch_optimizer_update(const OptimizerRule& r, int count, float* th
 // Record the message nsgb_last_error() returns on this host thread.
 void set_last_error(const char* msg);
 
+// Raise `kernel`'s dynamic shared-memory limit to everything the current
+// device allows beside its static shared memory.  Done once per (kernel,
+// device) under a lock, and never lowered afterwards, so launches of the same
+// kernel with different sizes from several host threads cannot race on the
+// limit.
+cudaError_t raise_smem_limit(const void* kernel);
+template <class K>
+inline cudaError_t raise_smem_limit(K* kernel) {
+  return raise_smem_limit(reinterpret_cast<const void*>(kernel));
+}
+
 }  // namespace nsgb

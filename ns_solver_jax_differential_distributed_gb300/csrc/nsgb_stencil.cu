@@ -477,7 +477,7 @@ static cudaError_t rows_config(K kernel, int N, int tw, int th, unsigned count, 
   const int W = rows::band_width(N, tw);
   smem = rows::smem_bytes(N, W, th);
   if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const cudaError_t e = raise_smem_limit(kernel);
     if (e != cudaSuccess) return e;
   }
   grid = dim3(N / W, (N + th - 1) / th, count);
@@ -525,12 +525,8 @@ static constexpr size_t stencil_smem() {
 
 template <int SCHEME, int MODE, int TW, int TH>
 static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_stencil<SCHEME, MODE, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         160 * 1024);
-    configured = true;
-  }
+  const cudaError_t e = raise_smem_limit(k_stencil<SCHEME, MODE, TW, TH>);
+  if (e != cudaSuccess) return e;
   const dim3 grid(a.c.N / TW, a.c.N / TH);
   k_stencil<SCHEME, MODE, TW, TH><<<grid, dim3(32, 8), stencil_smem<TW, TH>(), st>>>(a);
   return cudaGetLastError();
@@ -539,12 +535,8 @@ static cudaError_t launch_stencil_t(const StencilArgs& a, cudaStream_t st) {
 template <int SCHEME, int TW, int TH>
 static cudaError_t launch_stencil_batch_t(const SolveDev* solves, int count, int variant, int step_off, int N,
                                           cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(k_stencil_batch<SCHEME, TW, TH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         160 * 1024);
-    configured = true;
-  }
+  const cudaError_t e = raise_smem_limit(k_stencil_batch<SCHEME, TW, TH>);
+  if (e != cudaSuccess) return e;
   const dim3 grid(N / TW, N / TH, count);
   k_stencil_batch<SCHEME, TW, TH><<<grid, dim3(32, 8), stencil_smem<TW, TH>(), st>>>(solves, variant,
                                                                                    step_off);

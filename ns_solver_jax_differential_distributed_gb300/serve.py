@@ -142,17 +142,20 @@ class Server:
             if item is None:
                 return
             r, nbytes = item
-            with torch.cuda.stream(stream):
-                u0 = self.u0.get(r.N, r.seed)
-                th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
-                J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
-                                                      want_u_final=False, own_workspace=True)
-                Jh, gh = J.to("cpu", non_blocking=True), g.to("cpu", non_blocking=True)
-                ev = torch.cuda.Event()
-                ev.record(stream)
-            ev.synchronize()
-            r.J, r.grad = float(Jh), gh.numpy().copy()
-            done_q.put((r, nbytes))
+            try:
+                with torch.cuda.stream(stream):
+                    u0 = self.u0.get(r.N, r.seed)
+                    th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
+                    J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
+                                                          want_u_final=False, own_workspace=True)
+                    Jh, gh = J.to("cpu", non_blocking=True), g.to("cpu", non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(stream)
+                ev.synchronize()
+                r.J, r.grad = float(Jh), gh.numpy().copy()
+                done_q.put((r, nbytes, None))
+            except Exception as exc:  # handed to the scheduler, which raises it
+                done_q.put((r, nbytes, exc))
 
     def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None):
         """Serve `requests` (sorted by arrival).  With realtime, arrivals
@@ -260,7 +263,11 @@ class Server:
                     still.append((ev, a))
             finishing = still
             while not grad_done.empty():
-                r, nb = grad_done.get()
+                r, nb, exc = grad_done.get()
+                if exc is not None:
+                    for _ in workers:
+                        grad_q.put(None)
+                    raise RuntimeError(f"gradient request {r.rid} (N={r.N}) failed") from exc
                 r.t_done = time.perf_counter() - t0
                 self.used -= nb
                 grads_inflight -= 1
