@@ -136,6 +136,32 @@ inline void host_twiddles(int N, float2* out) {
   }
 }
 
+// a[s] = buffer[pad(j + s*T)], s = 0..E-1 (and the store of the same
+// positions): with T a multiple of 16 the padded positions are pad(j) plus
+// constants.
+template <int T, int E>
+__device__ __forceinline__ void load_strided(float2 (&a)[E], const float2* __restrict__ sb, int j) {
+  if constexpr (T % 16 == 0) {
+    const float2* src = sb + pad(j);
+#pragma unroll
+    for (int s = 0; s < E; ++s) a[s] = src[s * (T + T / 16)];
+  } else {
+#pragma unroll
+    for (int s = 0; s < E; ++s) a[s] = sb[pad(j + s * T)];
+  }
+}
+template <int T, int E>
+__device__ __forceinline__ void store_strided(const float2 (&a)[E], float2* __restrict__ sb, int j) {
+  if constexpr (T % 16 == 0) {
+    float2* dst = sb + pad(j);
+#pragma unroll
+    for (int s = 0; s < E; ++s) dst[s * (T + T / 16)] = a[s];
+  } else {
+#pragma unroll
+    for (int s = 0; s < E; ++s) sb[pad(j + s * T)] = a[s];
+  }
+}
+
 // One Stockham pass (stride NS) and, recursively, the remaining passes.
 template <int N, int NS, bool INV, int E>
 __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, int j,
@@ -197,14 +223,21 @@ __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, in
       for (int r = 0; r < RP; ++r) a[q + r * Q] = x[r];
     } else {
       const int base = (b / NS) * (NS * RP) + (b & (NS - 1));
+      if constexpr (NS == 1 || NS % 16 == 0) {
+        // base + r stays inside one 16-entry block (NS = 1) or r * NS is a
+        // multiple of 16: the padded positions are pad(base) plus constants
+        float2* dst = sb + pad(base);
 #pragma unroll
-      for (int r = 0; r < RP; ++r) sb[pad(base + r * NS)] = x[r];
+        for (int r = 0; r < RP; ++r) dst[r * (NS + NS / 16)] = x[r];
+      } else {
+#pragma unroll
+        for (int r = 0; r < RP; ++r) sb[pad(base + r * NS)] = x[r];
+      }
     }
   }
   if constexpr (!LAST) {
     __syncthreads();
-#pragma unroll
-    for (int s = 0; s < E; ++s) a[s] = sb[pad(j + s * T)];
+    load_strided<T, E>(a, sb, j);
     __syncthreads();
     pass<N, NS * RP, INV, E>(a, sb, j, tw);
   }

@@ -55,23 +55,35 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   for (int s = 0; s < E; ++s) a[s] = make_float2(__ldcs(ra + j + s * T), __ldcs(rb + j + s * T));
   fft::block_fft<N, false, E>(a, sb, j, tw);
   __syncthreads();
-#pragma unroll
-  for (int s = 0; s < E; ++s) sb[pad(j + s * T)] = a[s];
+  fft::store_strided<T, E>(a, sb, j);
   __syncthreads();
 
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
   const int lrb = __ffs(RB) - 1;  // RB is a power of two
-  for (int e = tid; e < RB * (H + 1); e += nth) {
-    const int r = e & (RB - 1);
-    const int k = e >> lrb;
+  // Element e = k * RB + r (row r of the CTA, frequency k) for e = tid, tid +
+  // nth, ...: with T even, nth is a multiple of RB, so a thread keeps its row
+  // r and steps k by nth / RB.
+  auto split = [&](int k, int r) {
     const float2* pb = smem2 + (r >> 1) * pair_stride<N>();
     const int kn = (N - k) & (N - 1);
     const float2 zk = pb[pad(k)], wk = pb[pad(kn)];
     const float zr = zk.x, zi = zk.y, wr = wk.x, wi = wk.y;
     // 2 X_a[k] = Z[k] + conj(Z[N-k]);  2 X_b[k] = -i (Z[k] - conj(Z[N-k]))
-    const float2 out = (r & 1) ? make_float2(zi + wi, wr - zr) : make_float2(zr + wr, zi - wi);
-    spec[(size_t)k * N + i0 + r] = out;
+    return (r & 1) ? make_float2(zi + wi, wr - zr) : make_float2(zr + wr, zi - wi);
+  };
+  if constexpr (T % 2 == 0) {
+    const int r = tid & (RB - 1);
+    const int kstep = nth >> lrb;
+    const size_t ostep = (size_t)kstep * N;
+    float2* out = spec + (size_t)(tid >> lrb) * N + i0 + r;
+    for (int k = tid >> lrb; k <= H; k += kstep, out += ostep) *out = split(k, r);
+  } else {
+    for (int e = tid; e < RB * (H + 1); e += nth) {
+      const int r = e & (RB - 1);
+      const int k = e >> lrb;
+      spec[(size_t)k * N + i0 + r] = split(k, r);
+    }
   }
 }
 
@@ -79,7 +91,8 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
 // Spectral multiplier  -1/(kx^2 + ky^2) * scale, 0 where the sum is 0.
 __device__ __forceinline__ float poisson_mult(float k2x, float k2y, float scale) {
   const float den = k2x + k2y;
-  const float inv = (den == 0.0f) ? 0.0f : __fdiv_rn(1.0f, den);
+  // __frcp_rn is the correctly rounded 1/den, the same float as 1.0f / den
+  const float inv = (den == 0.0f) ? 0.0f : __frcp_rn(den);
   return -inv * scale;
 }
 
@@ -141,18 +154,47 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     smem2[(r >> 1) * pair_stride<N>() + pad((r & 1) * (H + 1) + k)] = v;
   };
   auto src = [&](int e) { return spec + (size_t)(e >> lrb) * N + i0 + (e & (RB - 1)); };
-  int e = tid;
-  for (; e + 7 * nth < tot; e += 8 * nth) {
-    float2 v[8];
+  if constexpr (T % 2 == 0) {
+    // nth is a multiple of RB: a thread keeps its row r and steps k by
+    // nth / RB (the same elements as the generic loop below)
+    const int r = tid & (RB - 1);
+    const int kstep = nth >> lrb;
+    const size_t sstep = (size_t)kstep * N;
+    float2* sbase = smem2 + (r >> 1) * pair_stride<N>();
+    const int off = (r & 1) * (H + 1);
+    const float2* sp = spec + (size_t)(tid >> lrb) * N + i0 + r;
+    int k = tid >> lrb;
+    for (; k + 7 * kstep <= H; k += 8 * kstep, sp += 8 * sstep) {
+      float2 v[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) v[u] = __ldcs(src(e + u * nth));
+      for (int u = 0; u < 8; ++u) v[u] = __ldcs(sp + u * sstep);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) stage(e + u * nth, v[u]);
+      for (int u = 0; u < 8; ++u) sbase[pad(off + k + u * kstep)] = v[u];
+    }
+    for (; k <= H; k += kstep, sp += sstep) sbase[pad(off + k)] = __ldcs(sp);
+  } else {
+    int e = tid;
+    for (; e + 7 * nth < tot; e += 8 * nth) {
+      float2 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldcs(src(e + u * nth));
+#pragma unroll
+      for (int u = 0; u < 8; ++u) stage(e + u * nth, v[u]);
+    }
+    for (; e < tot; e += nth) stage(e, __ldcs(src(e)));
   }
-  for (; e < tot; e += nth) stage(e, __ldcs(src(e)));
   __syncthreads();
 
   float2* sb = smem2 + pp * pair_stride<N>();
+  // Padded positions of m, H+1+m, N-m and H+1+N-m for m = j + s*T: with T a
+  // multiple of 16 each is a per-thread base plus s times a constant.
+  constexpr bool kConst = (T % 16 == 0);
+  constexpr int TP = T + T / 16;
+  const int ia = pad(j), ib = pad(H + 1 + j), ic = pad(N - j), id = pad(H + 1 + N - j);
+  auto at_m = [&](int s, int m) { return kConst ? sb[ia + s * TP] : sb[pad(m)]; };
+  auto at_hm = [&](int s, int m) { return kConst ? sb[ib + s * TP] : sb[pad(H + 1 + m)]; };
+  auto at_nm = [&](int s, int m) { return kConst ? sb[ic - s * TP] : sb[pad(N - m)]; };
+  auto at_hnm = [&](int s, int m) { return kConst ? sb[id - s * TP] : sb[pad(H + 1 + N - m)]; };
   float2 a[E];
 #pragma unroll
   for (int s = 0; s < E; ++s) {
@@ -161,14 +203,14 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     if (m == 0 || m == H) {
       // DC and Nyquist of a real row are real: their imaginary parts (rounding
       // noise of the column pass) are dropped, as Re(ifft2) drops them.
-      z = make_float2(sb[pad(m)].x, sb[pad(H + 1 + m)].x);
+      z = make_float2(at_m(s, m).x, at_hm(s, m).x);
     } else if (m < H) {
-      const float2 xa = sb[pad(m)];
-      const float2 xb = sb[pad(H + 1 + m)];
+      const float2 xa = at_m(s, m);
+      const float2 xb = at_hm(s, m);
       z = make_float2(xa.x - xb.y, xa.y + xb.x);  // X_a + i X_b
     } else {
-      const float2 xa = sb[pad(N - m)];
-      const float2 xb = sb[pad(H + 1 + N - m)];
+      const float2 xa = at_nm(s, m);
+      const float2 xb = at_hnm(s, m);
       z = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj(X_a) + i conj(X_b)
     }
     a[s] = z;
