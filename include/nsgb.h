@@ -10,7 +10,7 @@
  *    field is (2, N, N): component 0 = u_x, 1 = u_y; axis 1 = x (rows, index i),
  *    axis 2 = y (contiguous, index j) -- the reference's layout
  *    (NS_solver.py:116, 676-679).
- *  - N is a power of two, 16 <= N <= 4096.
+ *  - N is a power of two, 16 <= N <= NSGB_MAX_N (8192).
  *  - Fields read by the step kernels (u, u0) must be 16-byte aligned (the
  *    kernels load them as float4 groups); a misaligned pointer is rejected
  *    with NSGB_ERR_INVALID_ARG.
@@ -42,6 +42,8 @@ extern "C" {
 #define NSGB_ERR_OOM 4
 #define NSGB_ERR_WORKSPACE 5
 #define NSGB_ERR_NONFINITE 6
+
+#define NSGB_MAX_N 8192 /* largest grid a plan accepts */
 
 #define NSGB_SCHEME_CENTRAL 0 /* CentralAdvection, NS_solver.py:468-477 */
 #define NSGB_SCHEME_UPWIND 1  /* UpwindAdvection,  NS_solver.py:480-488 */

@@ -537,8 +537,8 @@ const char* nsgb_last_error(void) { return g_last_error.c_str(); }
 int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
   *out = nullptr;
-  if (!is_pow2(N) || N < 16 || N > 4096)
-    return fail(NSGB_ERR_UNSUPPORTED_N, "N=%d unsupported: power of two in [16, 4096] required", N);
+  if (!is_pow2(N) || N < 16 || N > NSGB_MAX_N)
+    return fail(NSGB_ERR_UNSUPPORTED_N, "N=%d unsupported: power of two in [16, %d] required", N, NSGB_MAX_N);
   if (!(std::isfinite(L) && L > 0)) return fail(NSGB_ERR_INVALID_ARG, "L must be positive and finite");
   nsgb_plan* p = new nsgb_plan();
   p->N = N;

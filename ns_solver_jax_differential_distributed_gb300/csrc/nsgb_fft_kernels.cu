@@ -351,6 +351,7 @@ static cudaError_t dispatch(int N, const FftLaunch& L, const SolveDev* sv, int c
     case 1024: return launch_poisson_fft<1024>(L, sv, count, st);
     case 2048: return launch_poisson_fft<2048>(L, sv, count, st);
     case 4096: return launch_poisson_fft<4096>(L, sv, count, st);
+    case 8192: return launch_poisson_fft<8192>(L, sv, count, st);
     default: return cudaErrorInvalidValue;
   }
 }

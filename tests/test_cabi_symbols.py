@@ -41,7 +41,7 @@ def test_version_and_argument_errors(lib):
     L = _native.lib()
     assert L.nsgb_version() == 10000
     h = ctypes.c_void_p()
-    for N in (100, 8, 8192, 0, -4):
+    for N in (100, 8, 16384, 0, -4):
         assert L.nsgb_plan_create(N, 1.0, ctypes.byref(h)) == 2  # NSGB_ERR_UNSUPPORTED_N
         assert b"unsupported" in L.nsgb_last_error()
     assert L.nsgb_plan_create(64, -1.0, ctypes.byref(h)) == 1

@@ -22,9 +22,11 @@ def nat(cuda_lib):
     return _native
 
 
-def _with_radix(nat, N, radix, fn):
+def _with_radix(nat, N, radix, fn, rows=None):
     plan = nat.get_plan(N, L, torch.device("cuda"))
     old_r, old_t = plan.fft_radix(), plan.tiles()
+    if rows is not None:
+        plan.set_tiles(old_t[0], old_t[1], rows, old_t[3])
     plan.set_fft_radix(*radix)
     try:
         out = fn()
@@ -35,7 +37,7 @@ def _with_radix(nat, N, radix, fn):
         plan.set_tiles(*old_t)
 
 
-@pytest.mark.parametrize("N", [16, 32, 64, 256, 1024, 4096])
+@pytest.mark.parametrize("N", [16, 32, 64, 256, 1024, 4096, 8192])
 def test_poisson_radix8_matches_radix16_and_oracle(nat, N):
     rng = np.random.default_rng(N)
     rhs = rng.standard_normal((N, N)).astype(np.float32)
@@ -43,8 +45,19 @@ def test_poisson_radix8_matches_radix16_and_oracle(nat, N):
     t = torch.from_numpy(rhs).cuda()
     p16 = _with_radix(nat, N, (16, 16), lambda: nat.op_poisson(t, L).clone())
     ref = O.poisson_solve(rhs.astype(np.float64), L / N)
-    for radix in ((8, 8), (8, 16), (16, 8)):
-        p = _with_radix(nat, N, radix, lambda: nat.op_poisson(t, L).clone())
+    radices, rows = ((8, 8), (8, 16), (16, 8)), None
+    if N == 8192:
+        # a radix-8 transform of 8192 takes 1024 threads: the column kernel
+        # allows 512 and the row kernels one row pair per CTA, so the plan
+        # refuses the radix-8 column pass and radix-8 rows need 2 rows per CTA
+        for bad in ((8, 8), (16, 8)):
+            with pytest.raises(nat.NativeError):
+                _with_radix(nat, N, bad, lambda: None, rows=2)
+        with pytest.raises(nat.NativeError):
+            _with_radix(nat, N, (8, 16), lambda: None, rows=4)
+        radices, rows = ((8, 16),), 2
+    for radix in radices:
+        p = _with_radix(nat, N, radix, lambda: nat.op_poisson(t, L).clone(), rows=rows)
         assert rel_l2(p16.double().cpu().numpy(), p.double().cpu().numpy()) < 2e-6, radix
         assert rel_l2(ref, p.double().cpu().numpy()) < 5e-6, radix
 

@@ -47,7 +47,7 @@ def test_stencils_bit_exact(nsgb, N, L):
     assert np.array_equal(ops.divergence(torch.from_numpy(u).cuda()).cpu().numpy(), O.divergence(u, dx))
 
 
-@pytest.mark.parametrize("N", [16, 32, 64, 128, 256, 512, 1024, 2048, 4096])
+@pytest.mark.parametrize("N", [16, 32, 64, 128, 256, 512, 1024, 2048, 4096, 8192])
 def test_poisson_matches_oracle(nsgb, N):
     dx = 2 * math.pi / N
     rhs = _field(N, N)

@@ -139,6 +139,39 @@ def test_full_size_N4096(nsgb, scheme):
     assert float(div.abs().max()) < 1e-2 * float(ua.abs().max()) / dx
 
 
+def test_largest_grid_N8192(nsgb):
+    """N=8192 (the largest plan): 2 steps against the float32 oracle, on the
+    row-streaming stencil and on the tiled one (the same bits)."""
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    w = PLAIN_SCALE_CENTRAL
+    N = 8192
+    u0 = spectral_u0(N, 32, 5)
+    th = theta_draw(w.nu, seed=5)
+    cfg = O.OracleConfig(N=N, L=w.L, nu=float(th[2]), dt=w.dt, steps=2, scheme="central")
+    J32, u32 = O.rollout(u0, th, cfg)
+    plan = _native.get_plan(N, w.L, torch.device("cuda"))
+    old = plan.tiles()
+    outs = []
+    try:
+        for tiles in ((2048, 54), (64, 16)):
+            plan.set_tiles(tiles[0], tiles[1], old[2], old[3])
+            s = make_solver(nsgb, N, w.L, float(th[2]), w.dt, 2, "central")
+            J, u = s.rollout(torch.from_numpy(u0).cuda(), torch.from_numpy(th).cuda())
+            outs.append(u.cpu())
+            assert rel_l2(u32, u.cpu().numpy()) < 1e-5
+            assert abs(float(J) - float(J32)) <= 1e-5 * abs(float(J32)) + 1e-9
+    finally:
+        plan.set_tiles(*old)
+    assert torch.equal(outs[0], outs[1])
+
+
+def test_plan_rejects_n_beyond_max(nsgb):
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    for N in (16384, 8, 96):
+        with pytest.raises(_native.NativeError):
+            _native.Plan(N, 1.0, torch.device("cuda"))
+
+
 def test_runner_writes_reference_speed_field(nsgb, golden, tmp_path, monkeypatch):
     """runner.main with the reference's sample config for N=128 writes the
     reference's output file, whose content matches the speed field the
