@@ -130,3 +130,41 @@ def test_two_entry_theta(nsgb):
     _, g2 = s.gradient(u0, torch.tensor([1.0, 0.5]).cuda())
     _, g3 = s.gradient(u0, torch.tensor([1.0, 0.5, 1e-2]).cuda())
     assert g2.shape == (2,) and torch.allclose(g2, g3[:2], rtol=1e-6, atol=0)
+
+
+def test_repeated_gradient_calls_replay_as_graph(nsgb):
+    """The second call of nsgb_rollout_grad with identical arguments is
+    captured as a graph and later calls replay it: every call gives the same
+    bits as the first (eager) call, and a graph replay reads the current
+    contents of its input buffers (theta changed in place)."""
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    N, L, steps, every = 64, 2 * math.pi, 40, 8
+    u0 = torch.from_numpy(spectral_u0(N, 8, 4)).cuda()
+    th = torch.tensor([0.9, 0.45, 2e-3], dtype=torch.float32, device="cuda")
+    plan = _native.get_plan(N, L, torch.device("cuda"))
+    nbytes = _native.lib().nsgb_rollout_grad_workspace_bytes(plan.handle, steps, every)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    J = torch.empty((), dtype=torch.float32, device="cuda")
+    g = torch.empty(3, dtype=torch.float32, device="cuda")
+    ph = _native.make_phys(L, 2e-3, 1e-3, "upwind")
+    st = _native.stream_of(u0.device)
+
+    def call():
+        import ctypes
+        _native.call("nsgb_rollout_grad", plan.handle, ctypes.byref(ph), _native.ptr(u0), _native.ptr(th), 3,
+                     steps, every, _native.GRAD_FORWARD | _native.GRAD_BACKWARD, _native.ptr(J), None,
+                     _native.ptr(g), None, _native.ptr(ws), ws.numel(), st)
+        torch.cuda.synchronize()
+        return J.clone(), g.clone()
+
+    first = call()
+    for _ in range(3):  # capture, then replays
+        again = call()
+        assert torch.equal(first[0], again[0]) and torch.equal(first[1], again[1])
+    th.copy_(torch.tensor([1.1, 0.5, 2e-3]))
+    replay = call()
+    eager = nsgb.SingleCoreNSSolver(nsgb.make_grid(N, L), nsgb.Phys(nu=2e-3, mu0=0.5, sigma0=0.1, C=1.0),
+                                    nsgb.Time(dt=1e-3, steps=steps), "upwind",
+                                    checkpoint_every=every).gradient(u0, th.clone())
+    assert torch.equal(replay[0], eager[0]) and torch.equal(replay[1], eager[1])
+    assert not torch.equal(replay[1], first[1])
