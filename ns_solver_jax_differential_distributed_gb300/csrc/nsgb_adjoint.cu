@@ -46,8 +46,8 @@ struct AdjointSmem {
   static constexpr int F_OFF = LY_OFF + SH * SW;  // fx for the SH rows
   static constexpr int DA_OFF = F_OFF + SH;        // dfx/dA, dfx/dB for the TH rows
   static constexpr int DB_OFF = DA_OFF + TH;
-  static constexpr int RED_OFF = (DB_OFF + TH + 1) & ~1;  // 24 doubles
-  static constexpr size_t BYTES = (size_t)RED_OFF * sizeof(float) + 24 * sizeof(double);
+  static constexpr int RED_OFF = (DB_OFF + TH + 1) & ~1;  // 3 x 8 double-floats
+  static constexpr size_t BYTES = (size_t)RED_OFF * sizeof(float) + 24 * sizeof(DFloat);
 };
 
 template <int SCHEME, int TW, int TH>
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   float* sF = sm + Lay::F_OFF;
   float* sDA = sm + Lay::DA_OFF;
   float* sDB = sm + Lay::DB_OFF;
-  double* sRed = reinterpret_cast<double*>(sm + Lay::RED_OFF);
+  DFloat* sRed = reinterpret_cast<DFloat*>(sm + Lay::RED_OFF);
   const StepConsts& c = a.c;
   const int N = c.N, M = N - 1;
   const size_t NN = (size_t)N * N;
@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
 
   // theta sensitivities of the interior cells: float over a thread's few
-  // cells, double across threads, blocks and steps (the nu term is a small
-  // difference of large contributions)
+  // cells, double-float across the block's threads, double across blocks and
+  // steps (the nu term is a small difference of large contributions)
   float fA = 0.f, fB = 0.f, fN = 0.f;
   forflat<TH, TW>(tid, [&](int r, int cc) {
     const int o = (r + 2) * W4 + (cc + 4);
@@ -153,7 +153,6 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     const float luy = ((sUy[o - W4] - oy) + (sUy[o + W4] - oy)) + ((sUy[o + 1] - oy) + (sUy[o - 1] - oy));
     fN = fmaf(sMx[o], lux, fmaf(sMy[o], luy, fN));
   });
-  double gA = (double)fA, gB = (double)fB, gN = (double)fN * ((double)dt * (double)c.rdx2);
 
   // lambda_s on rows i0-1 .. i0+TH, columns j0-1 .. j0+TW
   forflat<SH, SW>(tid, [&](int r, int cc) {
@@ -212,9 +211,9 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
     });
   }
 
-  gA = warp_sum_d(gA);
-  gB = warp_sum_d(gB);
-  gN = warp_sum_d(gN);
+  const DFloat gA = warp_sum_df({fA, 0.f});
+  const DFloat gB = warp_sum_df({fB, 0.f});
+  const DFloat gN = warp_sum_df({fN, 0.f});
   if (tx == 0) {
     sRed[ty] = gA;
     sRed[8 + ty] = gB;
@@ -222,18 +221,17 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
   }
   __syncthreads();
   if (ty == 0) {
-    double v0 = (tx < 8) ? sRed[tx] : 0.0;
-    double v1 = (tx < 8) ? sRed[8 + tx] : 0.0;
-    double v2 = (tx < 8) ? sRed[16 + tx] : 0.0;
-    v0 = warp_sum_d(v0);
-    v1 = warp_sum_d(v1);
-    v2 = warp_sum_d(v2);
+    const DFloat z = {0.f, 0.f};
+    const DFloat v0 = warp_sum_df(tx < 8 ? sRed[tx] : z);
+    const DFloat v1 = warp_sum_df(tx < 8 ? sRed[8 + tx] : z);
+    const DFloat v2 = warp_sum_df(tx < 8 ? sRed[16 + tx] : z);
     if (tx == 0) {
       const int nblk = gridDim.x * gridDim.y;
       double* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
-      gp[0] = v0;
-      gp[1] = v1;
-      gp[2] = v2;
+      gp[0] = (double)v0.hi + (double)v0.lo;
+      gp[1] = (double)v1.hi + (double)v1.lo;
+      // the nu partial carries the Laplacian's 1/dx^2 and the step's dt
+      gp[2] = ((double)v2.hi + (double)v2.lo) * ((double)dt * (double)c.rdx2);
     }
   }
 }
@@ -261,41 +259,45 @@ cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
                                          : launch_adjoint_s<NSGB_SCHEME_UPWIND>(a, st);
 }
 
-// Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double).
-__global__ void k_greduce(const double* __restrict__ gpart, int nblk, int nrows,
-                          double* __restrict__ gacc) {
+// Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double):
+// one CTA per row sums the row's blocks by a fixed tree, then one thread adds
+// the row sums to gacc in row order.
+__global__ void k_greduce_rows(const double* __restrict__ gpart, int nblk, double* __restrict__ rowsum) {
   __shared__ double red[3][256];
-  for (int row = 0; row < nrows; ++row) {
-    const double* base = gpart + (size_t)row * nblk * 3;
-    double v0 = 0, v1 = 0, v2 = 0;
-    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-      v0 += base[3 * b];
-      v1 += base[3 * b + 1];
-      v2 += base[3 * b + 2];
-    }
-    red[0][threadIdx.x] = v0;
-    red[1][threadIdx.x] = v1;
-    red[2][threadIdx.x] = v2;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) {
-        red[0][threadIdx.x] += red[0][threadIdx.x + s];
-        red[1][threadIdx.x] += red[1][threadIdx.x + s];
-        red[2][threadIdx.x] += red[2][threadIdx.x + s];
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      gacc[0] += red[0][0];
-      gacc[1] += red[1][0];
-      gacc[2] += red[2][0];
+  const double* base = gpart + (size_t)blockIdx.x * nblk * 3;
+  double v0 = 0, v1 = 0, v2 = 0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+    v0 += base[3 * b];
+    v1 += base[3 * b + 1];
+    v2 += base[3 * b + 2];
+  }
+  red[0][threadIdx.x] = v0;
+  red[1][threadIdx.x] = v1;
+  red[2][threadIdx.x] = v2;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + s];
+      red[1][threadIdx.x] += red[1][threadIdx.x + s];
+      red[2][threadIdx.x] += red[2][threadIdx.x + s];
     }
     __syncthreads();
   }
+  if (threadIdx.x < 3) rowsum[3 * blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
 }
 
-cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st) {
-  if (nrows > 0) k_greduce<<<1, 256, 0, st>>>(gpart, nblk, nrows, gacc);
+__global__ void k_greduce_acc(const double* __restrict__ rowsum, int nrows, double* __restrict__ gacc) {
+  if (threadIdx.x >= 3) return;
+  double g = gacc[threadIdx.x];
+  for (int row = 0; row < nrows; ++row) g += rowsum[3 * row + threadIdx.x];
+  gacc[threadIdx.x] = g;
+}
+
+cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* rowsum, double* gacc,
+                           cudaStream_t st) {
+  if (nrows <= 0) return cudaSuccess;
+  k_greduce_rows<<<nrows, 256, 0, st>>>(gpart, nblk, rowsum);
+  k_greduce_acc<<<1, 32, 0, st>>>(rowsum, nrows, gacc);
   return cudaGetLastError();
 }
 

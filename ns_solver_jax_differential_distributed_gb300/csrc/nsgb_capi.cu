@@ -261,7 +261,7 @@ RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
 struct GradWs {
   RolloutWs f;
   float *ckpt, *ustore, *lamA, *lamB, *padj;
-  double *gpart, *gacc;
+  double *gpart, *growsum, *gacc;
   size_t bytes;
 };
 
@@ -284,6 +284,7 @@ GradWs carve_grad(const nsgb_plan* plan, int steps, int every, void* ws) {
   g.lamB = cv.take<float>(2 * NN);
   g.padj = cv.take<float>(NN);
   g.gpart = cv.take<double>((size_t)kGradRows * nblk * 3);
+  g.growsum = cv.take<double>((size_t)kGradRows * 3);
   g.gacc = cv.take<double>(4);
   g.bytes = cv.off;
   return g;
@@ -977,7 +978,7 @@ int grad_enqueue(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, 
       b.gslot = grow;
       NSGB_CUDA(launch_adjoint_stencil(b, st));
       if (++grow == kGradRows) {
-        NSGB_CUDA(launch_greduce(g.gpart, adj_nblk, grow, g.gacc, st));
+        NSGB_CUDA(launch_greduce(g.gpart, adj_nblk, grow, g.growsum, g.gacc, st));
         grow = 0;
       }
       if (s > 0) {
@@ -987,7 +988,7 @@ int grad_enqueue(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, 
       lam = lam_out;
     }
   }
-  NSGB_CUDA(launch_greduce(g.gpart, adj_nblk, grow, g.gacc, st));
+  NSGB_CUDA(launch_greduce(g.gpart, adj_nblk, grow, g.growsum, g.gacc, st));
   NSGB_CUDA(launch_gfinal(g.gacc, theta_len, dJdtheta, st));
   return NSGB_OK;
 }

@@ -190,4 +190,32 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// A double-float value hi + lo (|lo| <= ulp(hi)/2): about 48 significant bits
+// from float operations, which run at the full FP32 rate where FP64 runs at a
+// small fraction of it.
+struct DFloat {
+  float hi, lo;
+};
+
+// hi + lo of a + b: Knuth's TwoSum of the high parts (an error-free
+// transformation, so the result does not depend on the operand order), the
+// low parts added to its error, renormalised by Dekker's FastTwoSum.
+__device__ __forceinline__ DFloat df_add(DFloat a, DFloat b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  const float t = __fadd_rn(__fadd_rn(a.lo, b.lo), e);
+  const float hi = __fadd_rn(s, t);
+  return {hi, __fsub_rn(t, __fsub_rn(hi, s))};
+}
+
+__device__ __forceinline__ DFloat warp_sum_df(DFloat v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const DFloat w = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = df_add(v, w);
+  }
+  return v;
+}
+
 }  // namespace nsgb

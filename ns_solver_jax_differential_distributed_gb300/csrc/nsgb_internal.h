@@ -125,7 +125,9 @@ struct AdjointArgs {
   StepConsts c;
 };
 cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
-cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* gacc, cudaStream_t st);
+// rowsum: nrows x 3 doubles of scratch
+cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* rowsum, double* gacc,
+                           cudaStream_t st);
 cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st);
 
 // ------------------------------------------------------------- optimiser --
