@@ -92,6 +92,16 @@ int nsgb_plan_get_tiles(const nsgb_plan* plan, int out[4]);
 int nsgb_plan_set_fft_radix(nsgb_plan* plan, int radix_rows, int radix_cols);
 int nsgb_plan_get_fft_radix(const nsgb_plan* plan, int out[2]);
 
+/* No counterpart in the reference (launch tuning).  Shape of the adjoint
+ * stencil in nsgb_rollout_grad: a tile of tw x th cells of the tiled kernel
+ * (tw <= 128, tw <= N, th <= N), or for tw >= 256 a band of min(tw, N)
+ * columns (tw a power of two <= 1024) by th rows of the row-streaming kernel;
+ * 0 keeps the current value.  lambda and dJ/du0 have the same bits for every
+ * shape; the theta sensitivities are summed per CTA, so they agree to
+ * rounding across shapes (and are reproducible for a fixed shape). */
+int nsgb_plan_set_adjoint_tiles(nsgb_plan* plan, int tw, int th);
+int nsgb_plan_get_adjoint_tiles(const nsgb_plan* plan, int out[2]);
+
 /* Bytes of workspace for nsgb_poisson / nsgb_projector_step / nsgb_step. */
 size_t nsgb_poisson_workspace_bytes(const nsgb_plan* plan);
 size_t nsgb_step_workspace_bytes(const nsgb_plan* plan);

@@ -73,6 +73,8 @@ SIGNATURES = {
     "nsgb_plan_get_tiles": ([_P, ctypes.POINTER(_I)], _I),
     "nsgb_plan_set_fft_radix": ([_P, _I, _I], _I),
     "nsgb_plan_get_fft_radix": ([_P, ctypes.POINTER(_I)], _I),
+    "nsgb_plan_set_adjoint_tiles": ([_P, _I, _I], _I),
+    "nsgb_plan_get_adjoint_tiles": ([_P, ctypes.POINTER(_I)], _I),
     "nsgb_poisson_workspace_bytes": ([_P], _S),
     "nsgb_step_workspace_bytes": ([_P], _S),
     "nsgb_rollout_workspace_bytes": ([_P, _I], _S),
@@ -168,6 +170,14 @@ class Plan:
 
     def set_fft_radix(self, rows=0, cols=0) -> None:
         call("nsgb_plan_set_fft_radix", self.handle, int(rows), int(cols))
+
+    def adjoint_tiles(self) -> tuple:
+        out = (_I * 2)()
+        call("nsgb_plan_get_adjoint_tiles", self.handle, out)
+        return tuple(out)
+
+    def set_adjoint_tiles(self, tw=0, th=0) -> None:
+        call("nsgb_plan_set_adjoint_tiles", self.handle, int(tw), int(th))
 
     def workspace(self, kind: str, nbytes: int, stream: int) -> torch.Tensor:
         """A cached uint8 workspace of at least nbytes for (kind, stream)."""

@@ -78,16 +78,22 @@ def row_band_shapes(N: int, sms: int) -> list:
     return out
 
 
+# widest band of the row-streaming adjoint kernel
+ADJ_ROWS_MAX_W = 1024
+
+
 def candidates(N: int, sms: int = 152) -> dict:
     st = [(w, h) for (w, h) in STENCIL_TILES if w <= N and h <= N]
+    adj = list(st)
     if N >= 256:
         st += row_band_shapes(N, sms)
+        adj += [(w, h) for (w, h) in row_band_shapes(N, sms) if w <= ADJ_ROWS_MAX_W]
     rows, cols = [], []
     for radix in RADIX_CHOICES:
         T = N // min(radix, N)
         rows += [(radix, r) for r in ROW_CHOICES if r <= N and (r // 2) * T <= 1024]
         cols += [(radix, c) for c in COL_CHOICES if c <= N // 2 and c * T <= 512]
-    return {"stencil": st, "rows": rows, "cols": cols}
+    return {"stencil": st, "rows": rows, "cols": cols, "adjoint": adj}
 
 
 def _apply(plan, best: dict) -> None:
@@ -95,6 +101,24 @@ def _apply(plan, best: dict) -> None:
     plan.set_tiles(best["tw"], best["th"], 2, 1)
     plan.set_fft_radix(best.get("radix_rows", 16), best.get("radix_cols", 16))
     plan.set_tiles(best["tw"], best["th"], best["rows"], best["cols"])
+    if "adj_tw" in best:
+        plan.set_adjoint_tiles(best["adj_tw"], best["adj_th"])
+
+
+def _time_adjoint(u0, th, L, nu, dt, scheme, reps: int, steps: int = 6) -> float:
+    """Mean device ms of one backward step (adjoint stencil + FFT passes),
+    every state stored (no recompute)."""
+    sess = _native.GradSession(u0, th, steps, 1, L, nu, dt, scheme)
+    sess.forward()
+    sess.backward(want_du0=False)
+    torch.cuda.synchronize(u0.device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        sess.backward(want_du0=False)
+    e1.record()
+    torch.cuda.synchronize(u0.device)
+    return e0.elapsed_time(e1) / (reps * steps)
 
 
 def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, reps: int = 5,
@@ -143,6 +167,16 @@ def tune(N: int, L: float = 2 * math.pi, scheme: str = "central", device=None, r
                    "cols": results["cols"][(rc, cols)]},
             "default": list(base) + list(base_radix)}
     _apply(plan, best)
+    # adjoint shapes: one backward step with the tuned FFT shapes
+    results["adjoint"] = {}
+    base_adj = plan.adjoint_tiles()
+    for (w, h) in cand["adjoint"]:
+        plan.set_adjoint_tiles(w, h)
+        results["adjoint"][(w, h)] = _time_adjoint(u0, th, L, nu, dt, scheme, max(2, reps // 2))
+    best["adj_tw"], best["adj_th"] = min(results["adjoint"], key=results["adjoint"].get)
+    best["ms"]["adjoint_step"] = results["adjoint"][(best["adj_tw"], best["adj_th"])]
+    best["default"] += list(base_adj)
+    plan.set_adjoint_tiles(best["adj_tw"], best["adj_th"])
     if verbose:
         print(f"autotune N={N} {scheme}: best {best}")
         for kind, res in results.items():

@@ -573,6 +573,16 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   p->tile_w = t[0];
   p->tile_h = t[1];
   tile_kernel_default(N, p->adj_w, p->adj_h);
+  if (N >= 1024) {
+    // the row-streaming adjoint: bands of 1024 columns, rows for about two
+    // CTAs per SM (measured faster than the tiles from N = 1024 on)
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device);
+    const int col_bands = N / NSGB_ADJ_ROWS_MAX_W;
+    const int row_bands = (2 * sms + col_bands - 1) / col_bands;
+    p->adj_w = NSGB_ADJ_ROWS_MAX_W;
+    p->adj_h = std::max(8, (N + row_bands - 1) / row_bands);
+  }
   p->rows_per_cta = t[2];
   p->cols_per_cta = t[3];
 
@@ -662,6 +672,29 @@ int nsgb_plan_get_fft_radix(const nsgb_plan* plan, int out[2]) {
   if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
   out[0] = plan->radix_rows;
   out[1] = plan->radix_cols;
+  return NSGB_OK;
+}
+
+int nsgb_plan_set_adjoint_tiles(nsgb_plan* plan, int tw, int th) {
+  if (int r = check_plan(plan)) return r;
+  tw = tw ? tw : plan->adj_w;
+  th = th ? th : plan->adj_h;
+  if (stencil_rows_mode(tw) ? !adjoint_rows_supported(plan->N, tw, th)
+                            : (!stencil_tile_supported(tw, th) || tw > plan->N || th > plan->N))
+    return fail(NSGB_ERR_INVALID_ARG,
+                "adjoint shape %dx%d invalid for N=%d: a tiled-kernel shape, or a row band of power-of-two "
+                "width in [%d, %d] and 1 <= rows <= N", tw, th, plan->N, NSGB_ROWS_MIN_W, NSGB_ADJ_ROWS_MAX_W);
+  std::lock_guard<std::mutex> lk(plan->mu);
+  plan->adj_w = tw;
+  plan->adj_h = th;
+  return NSGB_OK;
+}
+
+int nsgb_plan_get_adjoint_tiles(const nsgb_plan* plan, int out[2]) {
+  if (int r = check_plan(plan)) return r;
+  if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
+  out[0] = plan->adj_w;
+  out[1] = plan->adj_h;
   return NSGB_OK;
 }
 

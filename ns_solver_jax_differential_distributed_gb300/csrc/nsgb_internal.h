@@ -125,6 +125,11 @@ struct AdjointArgs {
   StepConsts c;
 };
 cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
+// Adjoint shapes with tw >= NSGB_ROWS_MIN_W select the row-streaming adjoint
+// kernel: bands of min(tw, N) columns (a power of two <= NSGB_ADJ_ROWS_MAX_W;
+// its five input rings bound the band) by th rows.
+constexpr int NSGB_ADJ_ROWS_MAX_W = 1024;
+bool adjoint_rows_supported(int N, int tw, int th);
 // rowsum: nrows x 3 doubles of scratch
 cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* rowsum, double* gacc,
                            cudaStream_t st);

@@ -17,6 +17,7 @@
 // explicitly rounded intrinsics, so they round exactly like the reference's
 // float32 array expressions.
 #include "nsgb_internal.h"
+#include "nsgb_rows.cuh"
 
 namespace nsgb {
 
@@ -222,51 +223,10 @@ constexpr int kPRing = 8;                    // p rows t-1 .. t+1+kAhead (power 
 constexpr int kURing = 4;                    // u* rows t .. t+kAhead (power of two)
 static_assert(kPRing >= kAhead + 3 && kURing >= kAhead + 1, "ring depth");
 
-__host__ __device__ inline int band_width(int N, int tw) { return tw < N ? tw : N; }
-__host__ __device__ inline int groups(int N, int W) { return W == N ? N / 4 : W / 4 + 2; }
-__host__ __device__ inline int threads(int N, int W) { return (groups(N, W) + 31) / 32 * 32; }
-// ring row: 4 pad floats, the W + 8 columns from j0 - 4 (W < N) or from -4
-// (W = N, wrapped copies at both ends), 4 pad floats
-__host__ __device__ inline int ring_stride(int W) { return W + 16; }
 // shared memory: rings, edges [2 slots][3 fields][2 sides][G], forcing rows,
 // 32 partial sums
 inline size_t smem_bytes(int N, int W, int RH) {
   return sizeof(float) * ((size_t)(kPRing + 2 * kURing) * ring_stride(W) + (size_t)12 * groups(N, W) + RH + 2 + 32);
-}
-
-// Input rows are read once: their copies carry an L2 evict-first policy, so
-// they do not push the FFT passes' fields out of L2.
-__device__ __forceinline__ uint64_t evict_first_policy() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ void cp16(float* dst_smem, const float* src, uint64_t pol) {
-  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(
-                   (unsigned)__cvta_generic_to_shared(dst_smem)),
-               "l"(src), "l"(pol)
-               : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int PENDING>
-__device__ __forceinline__ void cp_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
-}
-
-__device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
-  *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
-}
-// Evict-first store, for u*next: it is read only by the next step's stencil,
-// after the FFT passes, so it should not push their inputs out of L2.
-__device__ __forceinline__ void st4_stream(float* __restrict__ base, size_t off, const float (&v)[4]) {
-  __stcs(reinterpret_cast<float4*>(base + off), make_float4(v[0], v[1], v[2], v[3]));
-}
-__device__ __forceinline__ void ld4s(const float* s, float (&o)[4]) {
-  const float4 v = *reinterpret_cast<const float4*>(s);
-  o[0] = v.x;
-  o[1] = v.y;
-  o[2] = v.z;
-  o[3] = v.w;
 }
 
 }  // namespace rows
