@@ -9,6 +9,11 @@ runs one warm step and then `reps` launches of each stage kernel with CUDA
 events (cold L2 per launch) and prints the mean time, the achieved bandwidth
 for the stage's algorithmic bytes and the fraction of the measured HBM peak.
 It launches few kernels, so it is the command to capture under ncu.
+
+    python -m ns_solver_jax_differential_distributed_gb300.profile_stages --N 4096 --scheme upwind --adjoint 6
+
+times the backward steps of a 6-step gradient (adjoint stencil and FFT passes
+per step, every state stored) instead.
 """
 from __future__ import annotations
 
@@ -136,6 +141,11 @@ def main(argv=None):
     ap.add_argument("--no-flush", action="store_true")
     ap.add_argument("--tiles", default="", help="tw,th,rows,cols")
     ap.add_argument("--radix", default="", help="FFT radix of the row and column passes: rows,cols")
+    ap.add_argument("--adjoint", type=int, default=0, metavar="STEPS",
+                    help="instead: time the backward steps of a STEPS-step gradient (every state stored)")
+    ap.add_argument("--adjoint-tiles", default="", help="tw,th of the adjoint stencil")
+    ap.add_argument("--tuned", action="store_true",
+                    help="apply the autotuner's cached shapes for (N, scheme) first (as bench.py runs them)")
     args = ap.parse_args(argv)
     _build.build()
     dev = torch.device("cuda")
@@ -143,10 +153,35 @@ def main(argv=None):
     u0 = torch.from_numpy(spectral_u0(args.N, min(32, args.N // 4), 0)).to(dev)
     th = torch.from_numpy(theta_draw(1e-4, 0)).to(dev)
     plan = _native.get_plan(args.N, L, dev)
+    if args.tuned:
+        from . import autotune
+        if not autotune.apply_cached(args.N, L, args.scheme, dev):
+            raise SystemExit(f"no cached autotune shapes for N={args.N} {args.scheme}")
     if args.radix:
         plan.set_fft_radix(*[int(x) for x in args.radix.split(",")])
     if args.tiles:
         plan.set_tiles(*[int(x) for x in args.tiles.split(",")])
+    if args.adjoint_tiles:
+        plan.set_adjoint_tiles(*[int(x) for x in args.adjoint_tiles.split(",")])
+    if args.adjoint:
+        # forward once, then `reps` backward phases (adjoint stencil + FFT
+        # passes per step), timed with CUDA events; few launches, so the
+        # command to capture the adjoint kernel under ncu
+        sess = _native.GradSession(u0, th, args.adjoint, 1, L, 1e-4, 2.5e-4, args.scheme)
+        sess.forward()
+        sess.backward(want_du0=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.reps):
+            g, _ = sess.backward(want_du0=False)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / (args.reps * args.adjoint)
+        print(json.dumps({"N": args.N, "scheme": args.scheme, "adjoint_tiles": plan.adjoint_tiles(),
+                          "tiles": plan.tiles(), "backward_step_ms": round(ms, 5),
+                          "dJdtheta": [float(x) for x in g.cpu()]}))
+        return
     flush = None if args.no_flush else torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     st = _native.time_stages(u0, th, L, 1e-4, 2.5e-4, args.scheme, args.reps, flush)
     try:
