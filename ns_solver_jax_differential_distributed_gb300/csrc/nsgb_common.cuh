@@ -184,12 +184,6 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-__device__ __forceinline__ double warp_sum_d(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // A double-float value hi + lo (|lo| <= ulp(hi)/2): about 48 significant bits
 // from float operations, which run at the full FP32 rate where FP64 runs at a
 // small fraction of it.
