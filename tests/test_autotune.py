@@ -58,7 +58,7 @@ def test_tune_applies_and_caches(cuda_lib, tmp_path, monkeypatch):
         assert len(cached) == 1 and next(iter(cached.values()))["adj_tw"] == best["adj_tw"]
         J1, u1 = _native.op_rollout(u0, th, 40, L, 1e-3, 1e-3, 0, 0.5, 0.1, 1.0, True)
         rel = float((u1 - u_ref).norm() / u_ref.norm())
-        assert rel < 1e-6, rel  # FFT radix and CTA shapes change rounding only
+        assert rel < 1e-5, rel  # FFT radix and CTA shapes change rounding only
         # a cached tuning is applied without timing
         plan.set_tiles(*old[0])
         assert autotune.apply_cached(N, L, "central", dev)
