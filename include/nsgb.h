@@ -230,6 +230,17 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
                      size_t flush_bytes, void* workspace, size_t workspace_bytes, float* out_ms,
                      void* stream);
 
+/* Measurement helper (no counterpart in the reference): runs `steps` solver
+ * steps from state u0 back to back on `stream`, as a rollout does, with a
+ * CUDA event between consecutive kernels, and writes the mean device time per
+ * launch of the four step kernels in milliseconds (out_ms as for
+ * nsgb_time_stages): the durations the kernels have inside the pipelined
+ * rollout, L2 shared between them.  Synchronises the stream.  Workspace:
+ * nsgb_rollout_workspace_bytes(plan, steps). */
+int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
+                            const float* theta, int theta_len, int steps, void* workspace,
+                            size_t workspace_bytes, float* out_ms, void* stream);
+
 /* Optimisers of ParameterOptimizationStudy (studies.py:879-884): optax
  * 0.2.4's sgd, adam and rmsprop, whose update rules nsgb_optim.cu restates. */
 #define NSGB_OPT_SGD 0

@@ -90,6 +90,7 @@ SIGNATURES = {
     "nsgb_rollout": ([_P, _PH, _P, _P, _I, _I, _P, _P, _P, _S, _I, _P], _I),
     "nsgb_rollout_grad": ([_P, _PH, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _P, _S, _P], _I),
     "nsgb_time_stages": ([_P, _PH, _P, _P, _I, _I, _P, _S, _P, _S, ctypes.POINTER(_F), _P], _I),
+    "nsgb_time_step_pipeline": ([_P, _PH, _P, _P, _I, _I, _P, _S, ctypes.POINTER(_F), _P], _I),
     "nsgb_ensemble_workspace_bytes": ([ctypes.POINTER(Member), _I], _S),
     "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
@@ -449,6 +450,23 @@ def time_stages(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: 
     call("nsgb_time_stages", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta), theta.numel(), int(reps),
          ptr(flush), 0 if flush is None else flush.numel() * flush.element_size(), ptr(ws), ws.numel(),
          out, st)
+    return dict(zip(STAGES, list(out)))
+
+
+def time_step_pipeline(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: float, scheme,
+                       steps: int = 20) -> dict:
+    """Mean device ms per launch of each stage kernel inside `steps`
+    back-to-back solver steps (CUDA events between consecutive kernels, L2
+    shared between them as in a rollout)."""
+    u0, theta = _cuda_f32(u0, "u0"), _cuda_f32(theta, "theta")
+    N = _square(u0, "u0", 2)
+    p = get_plan(N, L, u0.device)
+    st = stream_of(u0.device)
+    ph = make_phys(L, nu, dt, scheme)
+    ws = p.workspace("time_pipe", lib().nsgb_rollout_workspace_bytes(p.handle, int(steps) + 1), st)
+    out = (_F * 4)()
+    call("nsgb_time_step_pipeline", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta), theta.numel(), int(steps),
+         ptr(ws), ws.numel(), out, st)
     return dict(zip(STAGES, list(out)))
 
 

@@ -1402,4 +1402,65 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
   return NSGB_OK;
 }
 
+int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta,
+                            int theta_len, int steps, void* workspace, size_t ws_bytes, float* out_ms,
+                            void* stream) {
+  if (int r = check_plan(plan)) return r;
+  if (int r = check_phys(phys)) return r;
+  if (int r = check_theta(theta, theta_len)) return r;
+  if (!u0 || !out_ms) return fail(NSGB_ERR_INVALID_ARG, "NULL pointer");
+  if (int r = check_field(u0, "u0")) return r;
+  if (steps < 1) return fail(NSGB_ERR_INVALID_ARG, "steps must be >= 1");
+  const size_t need = carve_rollout(plan, steps + 1, nullptr).bytes;
+  if (int r = check_ws(workspace, ws_bytes, need)) return r;
+  RolloutWs w = carve_rollout(plan, steps + 1, workspace);
+  cudaStream_t st = (cudaStream_t)stream;
+  StencilArgs a = stencil_args(plan, phys);
+  a.theta = theta;
+  a.theta_len = theta_len;
+  // first step from u0 (p not yet pending), then `steps` timed steps
+  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, true, st));
+  std::vector<cudaEvent_t> ev((size_t)steps * 4 + 1, nullptr);
+  cudaError_t err = cudaSuccess;
+  for (auto& e : ev)
+    if (err == cudaSuccess) err = cudaEventCreate(&e);
+  const float* cur = w.usA;
+  for (int s = 0; s < steps && err == cudaSuccess; ++s) {
+    float* out = (cur == w.usA) ? w.usB : w.usA;
+    StencilArgs b = a;
+    b.us = cur;
+    b.p = w.p;
+    b.us_out = out;
+    b.rhs = w.rhs;
+    b.jpart = w.jpart;
+    b.jpart_rows = w.steps;
+    b.step_fixed = s + 1;
+    if (s == 0) err = cudaEventRecord(ev[0], st);
+    if (err == cudaSuccess) err = launch_stencil(b, MODE_ROLLOUT, st);
+    for (int stage = 1; stage <= 4 && err == cudaSuccess; ++stage) {
+      err = cudaEventRecord(ev[(size_t)s * 4 + stage], st);
+      if (err != cudaSuccess || stage == 4) break;
+      FftLaunch L = fft_launch(plan, w.rhs, w.spec, w.p);
+      if (stage != 1) L.rhs = nullptr;
+      L.do_cols = (stage == 2);
+      if (stage != 3) L.p = nullptr;
+      err = poisson_fft(plan->N, L, st);
+    }
+    cur = out;
+  }
+  double tot[4] = {0, 0, 0, 0};
+  if (err == cudaSuccess) err = cudaEventSynchronize(ev.back());
+  for (int s = 0; s < steps && err == cudaSuccess; ++s)
+    for (int k = 0; k < 4 && err == cudaSuccess; ++k) {
+      float ms = 0.f;
+      err = cudaEventElapsedTime(&ms, ev[(size_t)s * 4 + k], ev[(size_t)s * 4 + k + 1]);
+      tot[k] += ms;
+    }
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  if (err != cudaSuccess) return cuda_fail(err, "nsgb_time_step_pipeline");
+  for (int k = 0; k < 4; ++k) out_ms[k] = (float)(tot[k] / steps);
+  return NSGB_OK;
+}
+
 }  // extern "C"

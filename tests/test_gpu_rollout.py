@@ -189,3 +189,26 @@ def test_runner_writes_reference_speed_field(nsgb, golden, tmp_path, monkeypatch
     speed = np.load(tmp_path / out["path"])
     assert speed.shape == (128, 128) and speed.dtype == np.float32
     assert rel_l2(ref, speed.astype(np.float64)) < 1e-6
+
+
+def test_time_step_pipeline_matches_rollout(nsgb):
+    """nsgb_time_step_pipeline (per-kernel times inside back-to-back steps,
+    the roofline timing of bench.py): positive, and summing to about the
+    per-step time of a graph-replayed rollout."""
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    N, L, nu, dt, steps = 1024, 2 * math.pi, 1e-4, 2.5e-4, 64
+    u0 = torch.from_numpy(spectral_u0(N, 32, 0)).cuda()
+    th = torch.from_numpy(theta_draw(nu, seed=0)).cuda()
+    st = _native.time_step_pipeline(u0, th, L, nu, dt, "central", steps=20)
+    assert set(st) == {"stencil", "rows_fwd", "cols", "rows_inv"} and all(v > 0 for v in st.values())
+    _native.op_rollout(u0, th, steps, L, nu, dt, 0, 0.5, 0.1, 1.0, True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        _native.op_rollout(u0, th, steps, L, nu, dt, 0, 0.5, 0.1, 1.0, True)
+    e1.record()
+    torch.cuda.synchronize()
+    per_step = e0.elapsed_time(e1) / (3 * steps)
+    ratio = sum(st.values()) / per_step
+    assert 0.5 < ratio < 2.0, (st, per_step)
