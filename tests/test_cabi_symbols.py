@@ -49,6 +49,17 @@ def test_version_and_argument_errors(lib):
     assert L.nsgb_rollout(None, None, None, None, 2, 1, None, None, None, 0, 0, None) == 1
     assert b"plan" in L.nsgb_last_error()
     assert L.nsgb_poisson_workspace_bytes(None) == 0
+    # launch-tuning and measurement entry points refuse a NULL plan before
+    # touching the device
+    out = (ctypes.c_int * 2)()
+    assert L.nsgb_plan_set_adjoint_tiles(None, 64, 16) == 1
+    assert L.nsgb_plan_get_adjoint_tiles(None, out) == 1
+    assert L.nsgb_plan_set_fft_radix(None, 16, 16) == 1
+    outf = (ctypes.c_float * 4)()
+    assert L.nsgb_time_step_pipeline(None, None, None, None, 2, 4, None, 0, outf, None) == 1
+    assert b"plan" in L.nsgb_last_error()
+    assert L.nsgb_rollout_grad(None, None, None, None, 2, 4, 1, 3, None, None, None, None, None, 0, None) == 1
+    assert L.nsgb_rollout_grad_workspace_bytes(None, 4, 1) == 0
 
 
 def test_misaligned_field_rejected_before_launch(lib):
