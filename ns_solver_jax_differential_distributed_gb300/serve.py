@@ -109,7 +109,7 @@ class _U0Cache:
 
 class Server:
     def __init__(self, device=None, hbm_budget: float = 150e9, slice_steps: int = 32,
-                 max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 4):
+                 max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 8):
         dev = torch.device(device or "cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
