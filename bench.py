@@ -343,7 +343,7 @@ def run_reference(args, world, rank):
     O.set_fft_workers(cores)
     u0, th = w.u0(), w.theta()
     cfg = O.OracleConfig(N=w.N, L=w.L, nu=w.nu, dt=w.dt, steps=w.steps, scheme=w.scheme)
-    warm = max(1, min(args.warmup, 2))
+    warm = max(1, min(args.warmup, 10))  # warm-up solver steps, bounded
     O.rollout(u0, th, cfg, steps=warm)
     steps = max(1, min(args.steps, 40))  # one solver step per bench step, bounded
     t0 = time.perf_counter()
