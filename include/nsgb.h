@@ -172,7 +172,12 @@ int nsgb_rollout(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, 
  * call must follow a forward call with the same arguments and workspace
  * (the checkpoints live in the workspace).  The forward phase writes *J and,
  * if non-NULL, u_final; the backward phase writes dJdtheta[theta_len] and, if
- * non-NULL, dJdu0 (2,N,N). */
+ * non-NULL, dJdu0 (2,N,N).  A call repeated with the same arguments (pointers,
+ * sizes, physics, launch shapes) is captured as one CUDA graph on its second
+ * use and replayed after that, with the same results; inside a caller's own
+ * stream capture the work is recorded eagerly.  Workspace:
+ * nsgb_rollout_grad_workspace_bytes(plan, steps, every) (it depends on the
+ * plan's adjoint shape). */
 int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
                       const float* theta, int theta_len, int steps, int every, int phases,
                       float* J, float* u_final, float* dJdtheta, float* dJdu0, void* workspace,
