@@ -1208,7 +1208,7 @@ int nsgb_optimize(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
                                   grad_bytes, stream))
       return r;
     NSGB_CUDA(cudaMemcpyAsync(objectives + k, o.J, sizeof(float), cudaMemcpyDeviceToDevice, st));
-    NSGB_CUDA(launch_optimizer_update(optimizer_rule(*opt, k + 1), k + 1, o.theta, o.grad, o.mu, o.nu,
+    NSGB_CUDA(launch_optimizer_update(optimizer_rule(*opt, k + 1), o.theta, o.grad, o.mu, o.nu,
                                       parameters + (size_t)(k + 1) * theta_len, theta_len, st));
   }
   // objective at the last parameters (the study evaluates it after each update)

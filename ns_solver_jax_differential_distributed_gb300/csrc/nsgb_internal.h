@@ -142,8 +142,8 @@ struct OptimizerRule {
   int kind;
   float lr, b1, b2, one_minus_b1, one_minus_b2, bc1, bc2, eps, eps_root, decay, one_minus_decay;
 };
-cudaError_t launch_optimizer_update(const OptimizerRule& r, int count, float* theta, const float* grad, float* mu,
-                                    float* nu, float* theta_copy, int n, cudaStream_t st);
+cudaError_t launch_optimizer_update(const OptimizerRule& r, float* theta, const float* grad, float* mu, float* nu,
+                                    float* theta_copy, int n, cudaStream_t st);
 
 // Record the message nsgb_last_error() returns on this host thread.
 void set_last_error(const char* msg);

@@ -14,7 +14,7 @@
 
 namespace nsgb {
 
-__global__ void k_optimizer_update(OptimizerRule r, int count, float* __restrict__ theta,
+__global__ void k_optimizer_update(OptimizerRule r, float* __restrict__ theta,
                                    const float* __restrict__ grad, float* __restrict__ mu,
                                    float* __restrict__ nu, float* __restrict__ theta_copy, int n) {
   const int k = threadIdx.x;
@@ -41,9 +41,9 @@ __global__ void k_optimizer_update(OptimizerRule r, int count, float* __restrict
   if (theta_copy) theta_copy[k] = t;
 }
 
-cudaError_t launch_optimizer_update(const OptimizerRule& r, int count, float* theta, const float* grad, float* mu,
+cudaError_t launch_optimizer_update(const OptimizerRule& r, float* theta, const float* grad, float* mu,
                                     float* nu, float* theta_copy, int n, cudaStream_t st) {
-  k_optimizer_update<<<1, 32, 0, st>>>(r, count, theta, grad, mu, nu, theta_copy, n);
+  k_optimizer_update<<<1, 32, 0, st>>>(r, theta, grad, mu, nu, theta_copy, n);
   return cudaGetLastError();
 }
 
