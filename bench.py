@@ -205,6 +205,15 @@ def launches_per_rollout(steps: int, use_graph: bool, chunk: int = 16) -> int:
     return n
 
 
+def plain_config(w, world: int) -> dict:
+    """The workload description both arms print (same keys, same values)."""
+    return {"workload": w.name, "N": w.N, "solver_steps_per_step": w.steps, "dt": w.dt, "nu": w.nu,
+            "scheme": w.scheme, "L": "2pi", "u0": f"seeded spectral |k|<={w.K}",
+            "theta": "[A,B,nu] within 20% of [1,0.5,nu]", "parallelism": f"replicas{world}",
+            "l2": "working set ~470 MB > L2 (no flush needed)",
+            "cell_steps_per_step": int(w.N * w.N * w.steps)}
+
+
 # --------------------------------------------------------------- our arm
 def run_ours(args, world, rank, local):
     import torch
@@ -311,13 +320,8 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w.name, "N": w.N, "solver_steps_per_step": w.steps, "dt": w.dt,
-                       "nu": w.nu, "scheme": w.scheme, "L": "2pi", "u0": f"seeded spectral |k|<={w.K}",
-                       "theta": "[A,B,nu] within 20% of [1,0.5,nu]", "parallelism": f"replicas{world}",
-                       "l2": "working set ~470 MB > L2 (no flush needed)",
-                       "tiles": {k: tiles.get(k, 16) for k in ("tw", "th", "rows", "cols", "radix_rows",
-                                                                "radix_cols")},
-                       "cell_steps_per_step": int(cells)},
+            "config": plain_config(w, world),
+            "tiles": {k: tiles.get(k, 16) for k in ("tw", "th", "rows", "cols", "radix_rows", "radix_cols")},
             "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
             "gpu_launches": launches_per_rollout(w.steps, True) * args.steps,
             "J": float(J),
@@ -355,7 +359,7 @@ def run_reference(args, world, rank):
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": steps, "warmup": warm, "ms_per_step": el / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w.name, "N": w.N, "scheme": w.scheme, "parallelism": "host cpu"},
+            "config": plain_config(w, world), "host": "cpu",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

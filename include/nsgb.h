@@ -294,6 +294,12 @@ int nsgb_optimize(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0,
  * NSGB_ERR_UNSUPPORTED_N.  It calls no cudaMalloc or cudaFree.  The first call
  * on a device resolves the arrays' device addresses (cudaGetSymbolAddress)
  * with that device current; make that first call before any stream capture.
+ * Those addresses are cached per device ordinal, i.e. for the runtime's
+ * primary context (the one torch uses); do not reuse them across a
+ * cudaDeviceReset or from a context the caller created itself.  A call whose
+ * stream is capturing returns NSGB_ERR_INVALID_ARG and enqueues nothing: its
+ * table uploads read shared host buffers that a later call may refill before
+ * a graph replay would read them.
  * All calls share the arrays, which keep the last call's contents: calls
  * whose work overlaps on the GPU (other streams or host threads) race and
  * must be serialised by the caller.  rhs and p are (N,N) float32 device

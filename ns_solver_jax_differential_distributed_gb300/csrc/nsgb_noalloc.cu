@@ -13,7 +13,12 @@
 // cannot use those array names as device addresses, so the first call on each
 // device, with that device current, asks cudaGetSymbolAddress for them and
 // caches the addresses; that first call should come before any stream
-// capture.  Every call then uploads the twiddle and wavenumber tables for its
+// capture.  The cache is keyed by device ordinal and so assumes the runtime's
+// primary context on that device (the context torch and the runtime API use);
+// a caller that resets the device or runs in a context of its own creation
+// must not share the cached addresses.  A call on a capturing stream is
+// refused with NSGB_ERR_INVALID_ARG and enqueues nothing.  Every call uploads
+// the twiddle and wavenumber tables for its
 // (N, L) from a static host buffer with cudaMemcpyToSymbolAsync and runs the
 // same three FFT kernels as nsgb_poisson.  Nothing needs clearing: the
 // forward row pass writes every spectrum entry before the column pass reads it.
@@ -93,6 +98,16 @@ extern "C" int nsgb_poisson_noalloc(int N, double L, const float* rhs, float* p,
   if (e != cudaSuccess) return fail(NSGB_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(NSGB_ERR_INVALID_ARG, "device %d out of range", dev);
   cudaStream_t st = (cudaStream_t)stream;
+  // A captured table upload would become a graph node that reads the shared
+  // host staging tables at replay time, after later calls may have refilled
+  // them for another (N, L): refuse instead of recording it.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if ((e = cudaStreamIsCapturing(st, &cap)) != cudaSuccess)
+    return fail(NSGB_ERR_CUDA, "cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(NSGB_ERR_INVALID_ARG,
+                "nsgb_poisson_noalloc does not run on a capturing stream (its table uploads read shared "
+                "host buffers); call nsgb_poisson with a plan inside captures");
 
   std::lock_guard<std::mutex> lk(g_mu);
   DevicePtrs& d = g_dev[dev];
