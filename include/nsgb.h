@@ -102,6 +102,23 @@ int nsgb_plan_get_fft_radix(const nsgb_plan* plan, int out[2]);
 int nsgb_plan_set_adjoint_tiles(nsgb_plan* plan, int tw, int th);
 int nsgb_plan_get_adjoint_tiles(const nsgb_plan* plan, int out[2]);
 
+/* No counterpart in the reference (launch choice).  rows > 0 makes
+ * nsgb_rollout run each step after the first as two kernels instead of four:
+ * a fused row kernel -- the inverse row FFT of the solved spectrum into p in
+ * shared memory, the stencil of SingleCoreNSSolver.step (NS_solver.py:727-730,
+ * ChorinProjector.step :671-697, with the projection of the previous step)
+ * and the forward row FFT of its div(u*)/dt -- then the column FFT with the
+ * Poisson multiplier (SpectralPoissonSolver.__call__, :523-527), so neither p
+ * nor the right-hand side is written to device memory between the kernels.
+ * Bands of `rows` rows (even); clusters of N/2048 CTAs split each row when N
+ * > 2048.  rows < 0 picks the band height that fits all clusters on the GPU
+ * in one wave; 0 restores the four-kernel step.  N in {1024, 2048, 4096}
+ * (NSGB_ERR_UNSUPPORTED_N otherwise).  The results are those of the
+ * four-kernel step with the row-streaming stencil of the same band (width
+ * min(N, 2048), `rows` rows) and radix-16 row transforms, bit for bit. */
+int nsgb_plan_set_fused(nsgb_plan* plan, int rows);
+int nsgb_plan_get_fused(const nsgb_plan* plan, int* rows);
+
 /* Bytes of workspace for nsgb_poisson / nsgb_projector_step / nsgb_step. */
 size_t nsgb_poisson_workspace_bytes(const nsgb_plan* plan);
 size_t nsgb_step_workspace_bytes(const nsgb_plan* plan);
@@ -226,7 +243,9 @@ int nsgb_ensemble_rollout(const nsgb_member* members, int count, int chunk, void
  * of one rollout step from state u0 `reps` times each on `stream`, each launch
  * bracketed by CUDA events, and writes the mean device time per launch in
  * milliseconds: out_ms[0] fused stencil, [1] row FFT forward, [2] column FFT
- * with the Poisson multiplier, [3] row FFT inverse.  When flush != NULL,
+ * with the Poisson multiplier, [3] row FFT inverse.  With the fused row
+ * kernel (nsgb_plan_set_fused) a step has two kernels: out_ms[0] the fused
+ * row kernel, [1] the column FFT, [2] and [3] zero.  When flush != NULL,
  * flush_bytes of it are overwritten before every timed launch (outside the
  * events) so each launch starts with a cold L2.  Synchronises the stream.
  * Workspace: nsgb_rollout_workspace_bytes(plan, 1). */

@@ -75,6 +75,8 @@ SIGNATURES = {
     "nsgb_plan_get_fft_radix": ([_P, ctypes.POINTER(_I)], _I),
     "nsgb_plan_set_adjoint_tiles": ([_P, _I, _I], _I),
     "nsgb_plan_get_adjoint_tiles": ([_P, ctypes.POINTER(_I)], _I),
+    "nsgb_plan_set_fused": ([_P, _I], _I),
+    "nsgb_plan_get_fused": ([_P, ctypes.POINTER(_I)], _I),
     "nsgb_poisson_workspace_bytes": ([_P], _S),
     "nsgb_step_workspace_bytes": ([_P], _S),
     "nsgb_rollout_workspace_bytes": ([_P, _I], _S),
@@ -179,6 +181,19 @@ class Plan:
 
     def set_adjoint_tiles(self, tw=0, th=0) -> None:
         call("nsgb_plan_set_adjoint_tiles", self.handle, int(tw), int(th))
+
+    def fused_rows(self) -> int:
+        """Row band of the fused row kernel (0: the four-kernel step)."""
+        out = _I()
+        call("nsgb_plan_get_fused", self.handle, ctypes.byref(out))
+        return int(out.value)
+
+    def set_fused(self, rows: int) -> None:
+        """rows > 0: fused row kernel with bands of `rows` rows; -1: the band
+        that fits every cluster on the GPU at once; 0: four-kernel step."""
+        with torch.cuda.device(self.device):
+            call("nsgb_plan_set_fused", self.handle, int(rows))
+        self._ws.clear()
 
     def workspace(self, kind: str, nbytes: int, stream: int) -> torch.Tensor:
         """A cached uint8 workspace of at least nbytes for (kind, stream)."""
@@ -430,10 +445,19 @@ class GradSession:
 
 
 STAGES = ("stencil", "rows_fwd", "cols", "rows_inv")
+FUSED_STAGES = ("fused", "cols")
 # Algorithmic bytes per cell of each stage (float32): stencil reads u* (8) and
 # p (4) and writes u* (8) and rhs (4); each FFT pass reads and writes the
-# half spectrum or the real field once (4 + 4).
-STAGE_BYTES_PER_CELL = {"stencil": 24, "rows_fwd": 8, "cols": 8, "rows_inv": 8}
+# half spectrum or the real field once (4 + 4); the fused row kernel reads u*
+# (8) and the solved half spectrum (4) and writes u* (8) and the new half
+# spectrum (4).
+STAGE_BYTES_PER_CELL = {"stencil": 24, "rows_fwd": 8, "cols": 8, "rows_inv": 8, "fused": 24}
+
+
+def _stage_dict(p: "Plan", out) -> dict:
+    if p.fused_rows() > 0:
+        return {"fused": float(out[0]), "cols": float(out[1])}
+    return dict(zip(STAGES, [float(x) for x in out]))
 
 
 def time_stages(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: float, scheme,
@@ -450,7 +474,7 @@ def time_stages(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: 
     call("nsgb_time_stages", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta), theta.numel(), int(reps),
          ptr(flush), 0 if flush is None else flush.numel() * flush.element_size(), ptr(ws), ws.numel(),
          out, st)
-    return dict(zip(STAGES, list(out)))
+    return _stage_dict(p, out)
 
 
 def time_step_pipeline(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: float, dt: float, scheme,
@@ -467,7 +491,7 @@ def time_step_pipeline(u0: torch.Tensor, theta: torch.Tensor, L: float, nu: floa
     out = (_F * 4)()
     call("nsgb_time_step_pipeline", p.handle, ctypes.byref(ph), ptr(u0), ptr(theta), theta.numel(), int(steps),
          ptr(ws), ws.numel(), out, st)
-    return dict(zip(STAGES, list(out)))
+    return _stage_dict(p, out)
 
 
 def optimize(theta0: torch.Tensor, steps: int, every: int, N: int, L: float, nu: float, dt: float, scheme,

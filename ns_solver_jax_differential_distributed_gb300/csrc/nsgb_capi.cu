@@ -61,7 +61,7 @@ struct GraphEntry {
   int chunk = 0;
   StepConsts c{};
   int scheme = 0;
-  int tiles[6] = {0, 0, 0, 0, 0, 0};
+  int tiles[7] = {0, 0, 0, 0, 0, 0, 0};
   cudaGraphExec_t exec = nullptr;
 };
 
@@ -89,6 +89,7 @@ struct nsgb_plan {
   int tile_w = 64, tile_h = 16, rows_per_cta = 8, cols_per_cta = 2;
   int adj_w = 64, adj_h = 16;  // tiled-kernel shape of the adjoint stencil
   int radix_rows = 16, radix_cols = 16;  // Stockham radix of the FFT passes
+  int fused_rows = 0;  // row band of the fused row kernel (0: the four-kernel step)
   cudaStream_t graph_stream = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   std::vector<GraphEntry> graphs;
@@ -231,16 +232,26 @@ struct Carver {
 };
 
 struct RolloutWs {
-  float *usA, *usB, *p, *rhs, *spec, *jpart;
+  float *usA, *usB, *p, *rhs, *spec, *spec2, *jpart;
   double* jsteps;
   int* ctr;
   int steps;  // rows of jpart
   size_t bytes;
 };
 
+// Objective partials per step of a rollout: one per CTA of its stencil
+// launches (the fused row kernel's grid when the plan uses it).
+int rollout_nblk(const nsgb_plan* plan) {
+  return plan->fused_rows > 0 ? fused_nblocks(plan->N, plan->fused_rows)
+                              : stencil_nblocks(plan->N, plan->tile_w, plan->tile_h);
+}
+
 RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
   const size_t NN = (size_t)plan->N * plan->N;
-  const int nblk = stencil_nblocks(plan->N, plan->tile_w, plan->tile_h);
+  // rows of partials wide enough for either grid: every caller indexes them
+  // with the block count of the kernels it launches
+  const int nblk = std::max(stencil_nblocks(plan->N, plan->tile_w, plan->tile_h),
+                            plan->fused_rows > 0 ? fused_nblocks(plan->N, plan->fused_rows) : 0);
   Carver cv(ws);
   RolloutWs w;
   // Buffers that captured graphs reference come first, at offsets that do
@@ -251,6 +262,7 @@ RolloutWs carve_rollout(const nsgb_plan* plan, int steps, void* ws) {
   w.p = cv.take<float>(NN);
   w.rhs = cv.take<float>(NN);
   w.spec = cv.take<float>(spec_floats(plan->N));
+  w.spec2 = cv.take<float>(spec_floats(plan->N));
   w.jpart = cv.take<float>((size_t)(steps > 0 ? steps : 1) * nblk);
   w.jsteps = cv.take<double>(steps > 0 ? steps : 1);
   w.steps = steps > 0 ? steps : 1;
@@ -526,6 +538,46 @@ cudaError_t rollout_step(const nsgb_plan* plan, StencilArgs a, const float* us_i
   return poisson_fft(plan->N, fft_launch(plan, w.rhs, w.spec, w.p), st);
 }
 
+// Band width of the fused row kernel: whole rows up to 2048 columns, else
+// 2048-column slices (one CTA of a cluster each).
+int fused_width(int N) { return N / fused_cluster(N); }
+
+// The row passes that bracket a fused rollout (the first step's forward rows,
+// the last step's inverse rows) use radix 16 like the fused kernel, so every
+// transform of the rollout rounds the same way.
+FftLaunch fused_fft_launch(const nsgb_plan* plan, const float* rhs, void* spec, float* p) {
+  FftLaunch L = fft_launch(plan, rhs, spec, p);
+  L.radix_rows = 16;
+  return L;
+}
+
+// One forward step in the fused form: the fused row kernel (inverse row FFT
+// of spec_in into p on chip, the stencil with the pending projection, forward
+// row FFT of its rhs into spec_out), then the column pass on spec_out.
+cudaError_t fused_step(const nsgb_plan* plan, const StencilArgs& a, const float* us_in, const float* spec_in,
+                       float* us_out, float* spec_out, const RolloutWs& w, int step_fixed, const int* ctr,
+                       cudaStream_t st) {
+  FusedArgs f;
+  f.a = a;
+  f.a.us = us_in;
+  f.a.p = nullptr;
+  f.a.us_out = us_out;
+  f.a.rhs = nullptr;
+  f.a.u_out = nullptr;
+  f.a.jpart = w.jpart;
+  f.a.jpart_rows = w.steps;
+  f.a.step_ctr = ctr;
+  f.a.step_fixed = step_fixed;
+  f.a.t_from_step = 1;
+  f.a.th = plan->fused_rows;
+  f.spec_in = (const float2*)spec_in;
+  f.spec_out = (float2*)spec_out;
+  f.tw = plan->tw;  // radix-16 tables first
+  cudaError_t e = launch_fused_rows(f, st);
+  if (e != cudaSuccess) return e;
+  return poisson_fft(plan->N, fused_fft_launch(plan, nullptr, spec_out, nullptr), st);
+}
+
 }  // namespace
 
 void nsgb::set_last_error(const char* msg) { g_last_error = msg; }
@@ -698,6 +750,35 @@ int nsgb_plan_get_adjoint_tiles(const nsgb_plan* plan, int out[2]) {
   return NSGB_OK;
 }
 
+int nsgb_plan_set_fused(nsgb_plan* plan, int rows) {
+  if (int r = check_plan(plan)) return r;
+  if (rows == 0) {
+    std::lock_guard<std::mutex> lk(plan->mu);
+    plan->fused_rows = 0;
+    return NSGB_OK;
+  }
+  if (!fused_supported(plan->N))
+    return fail(NSGB_ERR_UNSUPPORTED_N, "the fused row kernel supports N in {1024, 2048, 4096} (N=%d)", plan->N);
+  if (rows < 0) {
+    const cudaError_t e = fused_default_rows(plan->N, rows);
+    if (e != cudaSuccess) return cuda_fail(e, "fused kernel occupancy");
+  }
+  if (rows < 2 || (rows & 1) || rows > plan->N)
+    return fail(NSGB_ERR_INVALID_ARG, "fused row band must be even and in [2, N] (got %d)", rows);
+  if (!stencil_rows_supported(plan->N, fused_width(plan->N), rows))
+    return fail(NSGB_ERR_INVALID_ARG, "fused row band %d not supported for N=%d", rows, plan->N);
+  std::lock_guard<std::mutex> lk(plan->mu);
+  plan->fused_rows = rows;
+  return NSGB_OK;
+}
+
+int nsgb_plan_get_fused(const nsgb_plan* plan, int* rows) {
+  if (int r = check_plan(plan)) return r;
+  if (!rows) return fail(NSGB_ERR_INVALID_ARG, "rows is NULL");
+  *rows = plan->fused_rows;
+  return NSGB_OK;
+}
+
 int nsgb_plan_get_tiles(const nsgb_plan* plan, int out[4]) {
   if (int r = check_plan(plan)) return r;
   if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
@@ -845,6 +926,13 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
   StencilArgs a = stencil_args(plan, phys);
   a.theta = theta;
   a.theta_len = theta_len;
+  // fused form: the first step's stencil uses the fused kernel's bands, so
+  // all steps write the same grid of objective partials
+  const bool fused = plan->fused_rows > 0;
+  if (fused) {
+    a.tw = fused_width(plan->N);
+    a.th = plan->fused_rows;
+  }
   const int nblk = stencil_nblocks(plan->N, a.tw, a.th);
 
   if (steps == 0) {
@@ -853,10 +941,13 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
     return NSGB_OK;
   }
 
-  // step 0 reads u0 directly; later steps ping-pong usA <-> usB.
-  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, true, st));
+  // step 0 reads u0 directly; later steps ping-pong usA <-> usB (and, fused,
+  // the half spectrum spec <-> spec2).
+  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, !fused, st));
+  if (fused) NSGB_CUDA(poisson_fft(plan->N, fused_fft_launch(plan, w.rhs, w.spec, nullptr), st));
   int s = 1;
   const float* cur = w.usA;
+  const float* spec_cur = w.spec;
   const int K = 16;  // steps per graph chunk (even: a chunk starts and ends in usA)
   if (use_graph && steps - 1 >= 2 * K) {
     std::lock_guard<std::mutex> lk(plan->mu);
@@ -866,7 +957,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
           g.scheme == a.scheme && std::memcmp(&g.c, &a.c, sizeof(StepConsts)) == 0 &&
           g.tiles[0] == plan->tile_w && g.tiles[1] == plan->tile_h && g.tiles[2] == plan->rows_per_cta &&
           g.tiles[3] == plan->cols_per_cta && g.tiles[4] == plan->radix_rows &&
-          g.tiles[5] == plan->radix_cols) {
+          g.tiles[5] == plan->radix_cols && g.tiles[6] == plan->fused_rows) {
         ge = &g;
         break;
       }
@@ -888,7 +979,11 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
       for (int k = 0; k < K && ce == cudaSuccess; ++k) {
         const float* in = (k % 2 == 0) ? w.usA : w.usB;
         float* out = (k % 2 == 0) ? w.usB : w.usA;
-        ce = rollout_step(plan, a, in, w.p, out, w, k, w.ctr, nullptr, true, gs);
+        if (fused)
+          ce = fused_step(plan, a, in, (k % 2 == 0) ? w.spec : w.spec2, out, (k % 2 == 0) ? w.spec2 : w.spec, w,
+                          k, w.ctr, gs);
+        else
+          ce = rollout_step(plan, a, in, w.p, out, w, k, w.ctr, nullptr, true, gs);
       }
       if (ce == cudaSuccess) ce = launch_step_counter(w.ctr, K, true, gs);
       cudaError_t ee = cudaStreamEndCapture(gs, &graph);
@@ -908,6 +1003,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
       g.tiles[3] = plan->cols_per_cta;
       g.tiles[4] = plan->radix_rows;
       g.tiles[5] = plan->radix_cols;
+      g.tiles[6] = plan->fused_rows;
       cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
       cudaGraphDestroy(graph);
       if (ie != cudaSuccess) return cuda_fail(ie, "cudaGraphInstantiate");
@@ -926,12 +1022,24 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
     NSGB_CUDA(cudaEventRecord(plan->ev_out, plan->graph_stream));
     NSGB_CUDA(cudaStreamWaitEvent(st, plan->ev_out, 0));
     cur = w.usA;
+    spec_cur = w.spec;
   }
   for (; s < steps; ++s) {
     const float* in = cur;
     float* out = (in == w.usA) ? w.usB : w.usA;
-    NSGB_CUDA(rollout_step(plan, a, in, w.p, out, w, s, nullptr, nullptr, true, st));
+    if (fused) {
+      float* spec_next = (spec_cur == w.spec) ? w.spec2 : w.spec;
+      NSGB_CUDA(fused_step(plan, a, in, spec_cur, out, spec_next, w, s, nullptr, st));
+      spec_cur = spec_next;
+    } else {
+      NSGB_CUDA(rollout_step(plan, a, in, w.p, out, w, s, nullptr, nullptr, true, st));
+    }
     cur = out;
+  }
+  if (fused) {  // p of the last step from its spectrum
+    FftLaunch L = fused_fft_launch(plan, nullptr, (void*)spec_cur, w.p);
+    L.do_cols = false;
+    NSGB_CUDA(poisson_fft(plan->N, L, st));
   }
   NSGB_CUDA(launch_project(cur, w.p, u_final, a.c, st));
   NSGB_CUDA(launch_jreduce(w.jpart, nblk, steps, w.jsteps, J, (double)phys->dt * (plan->L / plan->N) *
@@ -1359,8 +1467,15 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
   StencilArgs a = stencil_args(plan, phys);
   a.theta = theta;
   a.theta_len = theta_len;
-  // Steady state: one step from u0 leaves u* in usA and p pending.
-  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, true, st));
+  const bool fused = plan->fused_rows > 0;
+  if (fused) {
+    a.tw = fused_width(plan->N);
+    a.th = plan->fused_rows;
+  }
+  // Steady state: one step from u0 leaves u* in usA and p pending (fused:
+  // the solved spectrum in spec).
+  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, !fused, st));
+  if (fused) NSGB_CUDA(poisson_fft(plan->N, fused_fft_launch(plan, w.rhs, w.spec, nullptr), st));
   cudaEvent_t e0, e1;
   NSGB_CUDA(cudaEventCreate(&e0));
   NSGB_CUDA(cudaEventCreate(&e1));
@@ -1371,7 +1486,24 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
       if (flush && flush_bytes) err = cudaMemsetAsync(flush, r & 0xff, flush_bytes, st);
       if (err == cudaSuccess) err = cudaEventRecord(e0, st);
       if (err != cudaSuccess) break;
-      if (stage == 0) {
+      if (fused) {
+        // stage 0: the fused row kernel; stage 1: the column pass; 2, 3: none
+        if (stage == 0) {
+          FusedArgs f;
+          f.a = a;
+          f.a.us = w.usA;
+          f.a.us_out = w.usB;
+          f.a.jpart = w.jpart;
+          f.a.jpart_rows = w.steps;
+          f.a.step_fixed = 0;
+          f.spec_in = (const float2*)w.spec;
+          f.spec_out = (float2*)w.spec2;
+          f.tw = plan->tw;
+          err = launch_fused_rows(f, st);
+        } else if (stage == 1) {
+          err = poisson_fft(plan->N, fused_fft_launch(plan, nullptr, w.spec2, nullptr), st);
+        }
+      } else if (stage == 0) {
         StencilArgs b = a;
         b.us = w.usA;
         b.p = w.p;
@@ -1418,8 +1550,15 @@ int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const 
   StencilArgs a = stencil_args(plan, phys);
   a.theta = theta;
   a.theta_len = theta_len;
+  const bool fused = plan->fused_rows > 0;
+  if (fused) {
+    a.tw = fused_width(plan->N);
+    a.th = plan->fused_rows;
+  }
   // first step from u0 (p not yet pending), then `steps` timed steps
-  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, true, st));
+  NSGB_CUDA(rollout_step(plan, a, u0, nullptr, w.usA, w, 0, nullptr, nullptr, !fused, st));
+  if (fused) NSGB_CUDA(poisson_fft(plan->N, fused_fft_launch(plan, w.rhs, w.spec, nullptr), st));
+  const float* spec_cur = w.spec;
   std::vector<cudaEvent_t> ev((size_t)steps * 4 + 1, nullptr);
   cudaError_t err = cudaSuccess;
   for (auto& e : ev)
@@ -1436,6 +1575,25 @@ int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const 
     b.jpart_rows = w.steps;
     b.step_fixed = s + 1;
     if (s == 0) err = cudaEventRecord(ev[0], st);
+    if (fused) {
+      // stages: the fused row kernel, the column pass (two empty stages)
+      float* spec_next = (spec_cur == w.spec) ? w.spec2 : w.spec;
+      FusedArgs f;
+      f.a = b;
+      f.a.p = nullptr;
+      f.a.rhs = nullptr;
+      f.spec_in = (const float2*)spec_cur;
+      f.spec_out = (float2*)spec_next;
+      f.tw = plan->tw;
+      if (err == cudaSuccess) err = launch_fused_rows(f, st);
+      if (err == cudaSuccess) err = cudaEventRecord(ev[(size_t)s * 4 + 1], st);
+      if (err == cudaSuccess) err = poisson_fft(plan->N, fused_fft_launch(plan, nullptr, spec_next, nullptr), st);
+      for (int stage = 2; stage <= 4 && err == cudaSuccess; ++stage)
+        err = cudaEventRecord(ev[(size_t)s * 4 + stage], st);
+      spec_cur = spec_next;
+      cur = out;
+      continue;
+    }
     if (err == cudaSuccess) err = launch_stencil(b, MODE_ROLLOUT, st);
     for (int stage = 1; stage <= 4 && err == cudaSuccess; ++stage) {
       err = cudaEventRecord(ev[(size_t)s * 4 + stage], st);

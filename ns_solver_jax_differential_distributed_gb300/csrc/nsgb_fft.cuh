@@ -162,8 +162,20 @@ __device__ __forceinline__ void store_strided(const float2 (&a)[E], float2* __re
   }
 }
 
+// Barrier of the threads that carry one transform: the whole CTA (BAR = 0)
+// or the NT threads of a warp group using hardware barrier BAR (kernels in
+// which other warps run other work at the same time).
+template <int BAR, int NT>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (BAR == 0) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
+  }
+}
+
 // One Stockham pass (stride NS) and, recursively, the remaining passes.
-template <int N, int NS, bool INV, int E>
+template <int N, int NS, bool INV, int E, int BAR = 0>
 __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, int j,
                                      const float2* __restrict__ tw) {
   static_assert(E == 16 || E == 8 || E == N, "radix");
@@ -236,21 +248,22 @@ __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, in
     }
   }
   if constexpr (!LAST) {
-    __syncthreads();
+    group_sync<BAR, T>();
     load_strided<T, E>(a, sb, j);
-    __syncthreads();
-    pass<N, NS * RP, INV, E>(a, sb, j, tw);
+    group_sync<BAR, T>();
+    pass<N, NS * RP, INV, E, BAR>(a, sb, j, tw);
   }
 }
 
 // Full FFT of length N (unnormalised; INV uses exp(+2 pi i ...)) in radix E,
-// with `tw` the radix-E tables.  Every thread of the CTA must call it: it
-// synchronises the block between passes.  On return the exchange buffer is
-// free for reuse without a further barrier only after the caller's next
-// __syncthreads.
-template <int N, bool INV, int E>
+// with `tw` the radix-E tables.  Every thread of the CTA (BAR = 0), or of the
+// N/E-thread warp group synchronised by barrier BAR, must call it: it
+// synchronises those threads between passes.  On return the exchange buffer
+// is free for reuse without a further barrier only after their next
+// synchronisation.
+template <int N, bool INV, int E, int BAR = 0>
 __device__ __forceinline__ void block_fft(float2 (&a)[E], float2* sb, int j, const float2* __restrict__ tw) {
-  pass<N, 1, INV, E>(a, sb, j, tw);
+  pass<N, 1, INV, E, BAR>(a, sb, j, tw);
 }
 
 }  // namespace fft

@@ -64,6 +64,24 @@ bool stencil_rows_supported(int N, int tw, int th);
 // when the forward stencil streams rows).
 void tile_kernel_default(int N, int& tw, int& th);
 
+// ---------------------------------------------------- fused row kernel --
+// One rollout step's row work in one launch (nsgb_fused.cu): inverse row FFT
+// of spec_in into p (on chip), the fused stencil (a.us -> a.us_out, objective
+// partial; a.th = rows per band, a.tw unused) and the forward row FFT of its
+// rhs into spec_out.  The column pass (k_cols) then runs on spec_out.
+struct FusedArgs {
+  StencilArgs a;
+  const float2* spec_in = nullptr;  // half spectrum after the previous step's column pass
+  float2* spec_out = nullptr;       // half spectrum of this step's rhs (row transforms only)
+  const float2* tw = nullptr;       // the plan's radix-16 twiddle tables
+};
+bool fused_supported(int N);
+int fused_cluster(int N);               // CTAs per cluster (= N / band width)
+int fused_nblocks(int N, int th);       // CTAs per launch (the objective partials per step)
+cudaError_t launch_fused_rows(const FusedArgs& f, cudaStream_t st);
+// Band height whose clusters all fit on the GPU at once (one CTA per SM).
+cudaError_t fused_default_rows(int N, int& rows);
+
 // ------------------------------------------------------------- ensembles --
 // Device-resident description of one member of an ensemble advanced by
 // batched launches (blockIdx.z / blockIdx.y = member).
