@@ -60,30 +60,19 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
 
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
-  const int lrb = __ffs(RB) - 1;  // RB is a power of two
-  // Element e = k * RB + r (row r of the CTA, frequency k) for e = tid, tid +
-  // nth, ...: with T even, nth is a multiple of RB, so a thread keeps its row
-  // r and steps k by nth / RB.
-  auto split = [&](int k, int r) {
-    const float2* pb = smem2 + (r >> 1) * pair_stride<N>();
-    const int kn = (N - k) & (N - 1);
-    const float2 zk = pb[pad(k)], wk = pb[pad(kn)];
-    const float zr = zk.x, zi = zk.y, wr = wk.x, wi = wk.y;
-    // 2 X_a[k] = Z[k] + conj(Z[N-k]);  2 X_b[k] = -i (Z[k] - conj(Z[N-k]))
-    return (r & 1) ? make_float2(zi + wi, wr - zr) : make_float2(zr + wr, zi - wi);
-  };
-  if constexpr (T % 2 == 0) {
-    const int r = tid & (RB - 1);
-    const int kstep = nth >> lrb;
-    const size_t ostep = (size_t)kstep * N;
-    float2* out = spec + (size_t)(tid >> lrb) * N + i0 + r;
-    for (int k = tid >> lrb; k <= H; k += kstep, out += ostep) *out = split(k, r);
-  } else {
-    for (int e = tid; e < RB * (H + 1); e += nth) {
-      const int r = e & (RB - 1);
-      const int k = e >> lrb;
-      spec[(size_t)k * N + i0 + r] = split(k, r);
-    }
+  const int lp = __ffs(P) - 1;  // P is a power of two
+  // Element e = k * P + q (row pair q of the CTA, frequency k) for e = tid,
+  // tid + nth, ...: both rows of a pair come from one read of Z[k] and
+  // Z[N-k] and leave in one 16-byte store; a warp's stores cover whole
+  // 32-byte sectors when P >= 2.
+  // 2 X_a[k] = Z[k] + conj(Z[N-k]);  2 X_b[k] = -i (Z[k] - conj(Z[N-k]))
+  for (int e = tid; e < P * (H + 1); e += nth) {
+    const int q = e & (P - 1);
+    const int k = e >> lp;
+    const float2* pb = smem2 + q * pair_stride<N>();
+    const float2 zk = pb[pad(k)], wk = pb[pad((N - k) & (N - 1))];
+    *reinterpret_cast<float4*>(spec + (size_t)k * N + i0 + 2 * q) =
+        make_float4(zk.x + wk.x, zk.y - wk.y, zk.y + wk.y, wk.x - zk.x);
   }
 }
 
@@ -143,39 +132,35 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   const int tid = threadIdx.y * T + threadIdx.x;
   const int nth = T * P;
 
-  // Stage the RB half-spectrum rows: pair buffer (r>>1) holds X_a[k] at k
-  // and X_b[k] at H + 1 + k, k = 0..H.  The strided loads are issued in
-  // batches of 8 before their shared-memory stores, so their latencies overlap.
-  const int tot = RB * (H + 1);
-  const int lrb = __ffs(RB) - 1;  // RB is a power of two
-  auto stage = [&](int e, float2 v) {
-    const int r = e & (RB - 1);
-    const int k = e >> lrb;
-    smem2[(r >> 1) * pair_stride<N>() + pad((r & 1) * (H + 1) + k)] = v;
-  };
-  auto src = [&](int e) { return spec + (size_t)(e >> lrb) * N + i0 + (e & (RB - 1)); };
-  if constexpr (T % 2 == 0) {
-    // nth is a multiple of RB: a thread keeps its row r and steps k by
-    // nth / RB (the same elements as the generic loop below)
-    const int r = tid & (RB - 1);
-    const int kstep = nth >> lrb;
-    const size_t sstep = (size_t)kstep * N;
-    float2* sbase = smem2 + (r >> 1) * pair_stride<N>();
-    const int off = (r & 1) * (H + 1);
-    const float2* sp = spec + (size_t)(tid >> lrb) * N + i0 + r;
-    int k = tid >> lrb;
-    for (; k + 7 * kstep <= H; k += 8 * kstep, sp += 8 * sstep) {
-      float2 v[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = __ldcs(sp + u * sstep);
-#pragma unroll
-      for (int u = 0; u < 8; ++u) sbase[pad(off + k + u * kstep)] = v[u];
+  // Stage Z[m] = X_a[m] + i X_b[m] of each row pair (m > N/2 from the
+  // conjugate symmetry of the two real rows: Z[N-k] = conj(X_a[k]) + i
+  // conj(X_b[k])) straight into the pair's exchange buffer: element e = k * P
+  // + q reads X_a[k], X_b[k] of pair q as one 16-byte load (a warp covers
+  // whole 32-byte sectors when P >= 2) and writes Z[k] and Z[N-k].  DC and
+  // Nyquist of a real row are real: their imaginary parts (rounding noise of
+  // the column pass) are dropped, as Re(ifft2) drops them.  The loads are
+  // issued in batches of 8 before their shared-memory stores, so their
+  // latencies overlap.
+  const int tot = P * (H + 1);
+  const int lp = __ffs(P) - 1;  // P is a power of two
+  auto stage = [&](int e, float4 v) {
+    const int q = e & (P - 1);
+    const int k = e >> lp;
+    float2* pb = smem2 + q * pair_stride<N>();
+    if (k == 0 || k == H) {
+      pb[pad(k)] = make_float2(v.x, v.z);
+    } else {
+      pb[pad(k)] = make_float2(v.x - v.w, v.y + v.z);
+      pb[pad(N - k)] = make_float2(v.x + v.w, v.z - v.y);
     }
-    for (; k <= H; k += kstep, sp += sstep) sbase[pad(off + k)] = __ldcs(sp);
-  } else {
+  };
+  auto src = [&](int e) {
+    return reinterpret_cast<const float4*>(spec + (size_t)(e >> lp) * N + i0 + 2 * (e & (P - 1)));
+  };
+  {
     int e = tid;
     for (; e + 7 * nth < tot; e += 8 * nth) {
-      float2 v[8];
+      float4 v[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) v[u] = __ldcs(src(e + u * nth));
 #pragma unroll
@@ -186,35 +171,8 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   __syncthreads();
 
   float2* sb = smem2 + pp * pair_stride<N>();
-  // Padded positions of m, H+1+m, N-m and H+1+N-m for m = j + s*T: with T a
-  // multiple of 16 each is a per-thread base plus s times a constant.
-  constexpr bool kConst = (T % 16 == 0);
-  constexpr int TP = T + T / 16;
-  const int ia = pad(j), ib = pad(H + 1 + j), ic = pad(N - j), id = pad(H + 1 + N - j);
-  auto at_m = [&](int s, int m) { return kConst ? sb[ia + s * TP] : sb[pad(m)]; };
-  auto at_hm = [&](int s, int m) { return kConst ? sb[ib + s * TP] : sb[pad(H + 1 + m)]; };
-  auto at_nm = [&](int s, int m) { return kConst ? sb[ic - s * TP] : sb[pad(N - m)]; };
-  auto at_hnm = [&](int s, int m) { return kConst ? sb[id - s * TP] : sb[pad(H + 1 + N - m)]; };
   float2 a[E];
-#pragma unroll
-  for (int s = 0; s < E; ++s) {
-    const int m = j + s * T;
-    float2 z;
-    if (m == 0 || m == H) {
-      // DC and Nyquist of a real row are real: their imaginary parts (rounding
-      // noise of the column pass) are dropped, as Re(ifft2) drops them.
-      z = make_float2(at_m(s, m).x, at_hm(s, m).x);
-    } else if (m < H) {
-      const float2 xa = at_m(s, m);
-      const float2 xb = at_hm(s, m);
-      z = make_float2(xa.x - xb.y, xa.y + xb.x);  // X_a + i X_b
-    } else {
-      const float2 xa = at_nm(s, m);
-      const float2 xb = at_hnm(s, m);
-      z = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj(X_a) + i conj(X_b)
-    }
-    a[s] = z;
-  }
+  fft::load_strided<T, E>(a, sb, j);
   __syncthreads();
   fft::block_fft<N, true, E>(a, sb, j, tw);
   float* ra = p + (size_t)(i0 + 2 * pp) * N;

@@ -15,7 +15,14 @@ summaries under tests/golden/:
   dt=1e-3, nu=5e-4, upwind): J in float32 and float64 and the central finite-
   difference gradient of the float64 oracle's J with respect to [A, B, nu]
   with relative steps 1e-3 and 5e-4 per parameter (the method of
-  studies.py:306-318; the two steps bound the truncation error).
+  studies.py:306-318; the two steps bound the truncation error), and for A
+  also with relative steps 1e-5 and 1e-7.  The forcing's period-1 wrap
+  d = (x - mu) - round(x - mu) (NS_solver.py:626) gives f_x a kink in mu at
+  every row and step; at this size thousands of them fall within +-1e-3 A,
+  so wide steps average the slope over kinks, while reverse-mode
+  differentiation (jax.grad, the discrete adjoint) returns the derivative at
+  the point, which the small steps resolve (1e-7 A sits between the kink
+  spacing and float64 noise).
 
 Each rollout runs in its own process of a spawn-started pool (the oracle's
 array code is single-threaded), one process per core by default.
@@ -42,6 +49,8 @@ from ns_solver_jax_differential_distributed_gb300.workloads import (  # noqa: E4
     GRAD_N1024, PLAIN_SCALE_CENTRAL, PLAIN_SCALE_UPWIND)
 
 SAMPLE_ROWS = 17 + 256 * np.arange(16)
+# (relative step, parameters) of the finite differences of the gradient case
+FD_STEPS = ((1e-3, (0, 1, 2)), (5e-4, (0, 1)), (1e-5, (0,)), (1e-7, (0,)))
 
 
 def _cfg(w):
@@ -86,7 +95,7 @@ def grad_jobs(w):
     th = w.theta().astype(np.float64)
     jobs = [(w.name, "f32", th.tolist(), False), (w.name, "f64", th.tolist(), False)]
     keys = [("J32",), ("J64",)]
-    for rs, params in ((1e-3, (0, 1, 2)), (5e-4, (0, 1))):
+    for rs, params in FD_STEPS:
         for i in params:
             h = rs * abs(th[i])
             for sgn in (1, -1):
@@ -105,7 +114,7 @@ def grad_summary(w, keys, results):
         vals[k] = J
         secs += s
     fd = {}
-    for rs, params in ((1e-3, (0, 1, 2)), (5e-4, (0, 1))):
+    for rs, params in FD_STEPS:
         g = []
         for i in params:
             kp = [k for k in keys if k[0] == "fd" and k[1] == rs and k[2] == i and k[3] == 1][0]
