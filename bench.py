@@ -370,10 +370,11 @@ def run_grad(args):
     dt=1e-3, nu=5e-4, upwind; time against the forward rollout and peak memory
     with checkpoints every 50 steps (recompute in the backward pass) and with
     the automatic policy (every state kept when the states fit in half the
-    free HBM: 8.4 GB here, no recompute); central finite differences of the
-    GPU float32 forward as a sanity check (relative steps 1e-4 for A, 1e-3
-    for B, 5e-2 for nu, whose sensitivity is below float32 resolution at
-    smaller steps)."""
+    free HBM: 8.4 GB here, no recompute).  The gradient is compared with the
+    float64 oracle's derivative at the same point (central differences with
+    relative steps 1e-7 for A -- the forcing's wrap puts kinks in J(A) closer
+    than 1e-3 A -- and 1e-3 for B and nu), read from the committed fixture
+    tests/golden/grad_N1024_upwind.json."""
     import torch
     import ns_solver_jax_differential_distributed_gb300 as nsgb
     from ns_solver_jax_differential_distributed_gb300 import _build, autotune
@@ -386,10 +387,11 @@ def run_grad(args):
                                      checkpoint_every=GRAD_CHECKPOINT_EVERY)
     u0 = torch.from_numpy(w.u0()).to(dev)
     th = torch.from_numpy(w.theta()).to(dev)
+    reps = max(1, args.steps)
 
-    def timed(fn, reps):
-        fn()
-        fn()  # a call repeated with the same arguments replays as a graph from here on
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()  # a call repeated with the same arguments replays as a graph from the second on
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -399,40 +401,42 @@ def run_grad(args):
         torch.cuda.synchronize(dev)
         return e0.elapsed_time(e1) / reps, out
 
+    clocks = ClockSampler(0).start()
     torch.cuda.reset_peak_memory_stats(dev)
-    t_fwd, (J, _) = timed(lambda: solver.rollout(u0, th), max(1, args.steps))
+    t_fwd, (J, _) = timed(lambda: solver.rollout(u0, th))
     mem_fwd = torch.cuda.max_memory_allocated(dev)
     torch.cuda.reset_peak_memory_stats(dev)
-    t_grad, (Jg, g) = timed(lambda: solver.gradient(u0, th), max(1, args.steps))
+    t_grad, (Jg, g) = timed(lambda: solver.gradient(u0, th))
     mem_grad = torch.cuda.max_memory_allocated(dev)
     solver_all = nsgb.SingleCoreNSSolver(nsgb.make_grid(w.N, w.L), nsgb.Phys(nu=w.nu, mu0=0.5, sigma0=0.1, C=1.0),
                                          nsgb.Time(dt=w.dt, steps=w.steps), w.scheme, device=dev)
     every_auto = solver_all._every()
     torch.cuda.reset_peak_memory_stats(dev)
-    t_all, (_, g_all) = timed(lambda: solver_all.gradient(u0, th), max(1, args.steps))
+    t_all, (_, g_all) = timed(lambda: solver_all.gradient(u0, th))
     mem_all = torch.cuda.max_memory_allocated(dev)
+    clock_info = clocks.stop()
     g = g.double().cpu().numpy()
-    th64 = th.double().cpu().numpy()
-    fd = []
-    for k, rs in enumerate((1e-4, 1e-3, 5e-2)):
-        h = rs * abs(th64[k])
-        tp, tm = th64.copy(), th64.copy()
-        tp[k] += h
-        tm[k] -= h
-        Jp = float(solver.rollout(u0, torch.tensor(tp, dtype=torch.float32, device=dev))[0])
-        Jm = float(solver.rollout(u0, torch.tensor(tm, dtype=torch.float32, device=dev))[0])
-        fd.append((Jp - Jm) / (2 * h))
-    cells = float(w.N) * w.N * w.steps
+    ref = None
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "grad_N1024_upwind.json")) as f:
+            fx = json.load(f)["fd64"]
+        ref = [fx["1e-07"][0], fx["0.001"][1], fx["0.001"][2]]
+    except (OSError, KeyError):
+        pass
     return {"metric": "adjoint gradient time / forward time", "value": t_grad / t_fwd, "unit": "x",
-            "higher_is_better": False, "workload": w.name, "N": w.N, "steps": w.steps, "scheme": w.scheme,
-            "checkpoint_every": GRAD_CHECKPOINT_EVERY, "forward_ms": t_fwd, "gradient_ms": t_grad,
-            "forward_cell_steps_per_s": cells / (t_fwd / 1e3), "J": float(Jg), "dJdtheta": g.tolist(),
-            "fd_gpu_float32": fd, "fd_rel_diff": [abs(a - b) / max(abs(b), 1e-30) for a, b in zip(g, fd)],
+            "higher_is_better": False,
+            "config": {"workload": w.name, "N": w.N, "steps": w.steps, "dt": w.dt, "nu": w.nu,
+                       "scheme": w.scheme, "L": "2pi", "u0": f"seeded spectral |k|<={w.K}",
+                       "checkpoint_every": GRAD_CHECKPOINT_EVERY},
+            "forward_ms": t_fwd, "gradient_ms": t_grad, "reps": reps,
+            "forward_cell_steps_per_s": float(w.N) * w.N * w.steps / (t_fwd / 1e3), "J": float(Jg),
+            "dJdtheta": g.tolist(), "float64_derivative": ref,
+            "rel_err_vs_float64": None if ref is None else [abs(a - b) / abs(b) for a, b in zip(g, ref)],
             "peak_mem_forward_bytes": mem_fwd, "peak_mem_gradient_bytes": mem_grad,
             "auto_checkpoint": {"checkpoint_every": every_auto, "gradient_ms": t_all,
                                 "ratio_to_forward": t_all / t_fwd, "peak_mem_gradient_bytes": mem_all,
                                 "max_abs_diff_vs_every_50": float(np.abs(g_all.double().cpu().numpy() - g).max())},
-            "dtype": "f32", "data": "synthetic"}
+            "clocks": clock_info, "dtype": "f32", "data": "synthetic"}
 
 
 def run_optimize(args):
@@ -458,16 +462,20 @@ def run_optimize(args):
     study.run_all()  # warm-up (plans, workspaces)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0).start()
     t0 = time.perf_counter()
     e0.record()
     res = study.run_all()
     e1.record()
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t0
+    clock_info = clocks.stop()
     n_steps = 4 * 100
     return {"metric": "optimiser steps/s", "value": n_steps / (e0.elapsed_time(e1) / 1e3), "unit": "steps/s",
             "higher_is_better": True, "ms_per_optimizer_step": e0.elapsed_time(e1) / n_steps,
-            "wall_s": wall, "config": {"N": N, "L": L, "nu": nu, "dt": dt, "steps": steps, "scheme": "central",
+            "wall_s": wall, "clocks": clock_info,
+            "config": {"workload": "optimiser study (studies.py:864-934)", "N": N, "L": L, "nu": nu, "dt": dt,
+                       "steps": steps, "scheme": "central",
                                        "theta0": [1.0, 0.5], "optim_steps": 100,
                                        "checkpoint_every": solver._every()},
             "final": {k: {"obj_initial": v["obj_initial"], "obj_final": v["obj_final"],
@@ -507,10 +515,14 @@ def run_ensemble(args):
         torch.cuda.synchronize(dev)
         return e0.elapsed_time(e1) / max(1, args.steps), out
 
+    clocks = ClockSampler(0).start()
     t_s, (Js, us) = timed(ens.run_sequential)
     Js, us = Js.clone(), [u.clone() for u in us]
+    seq_clocks = clocks.stop()
     ens.tune_batched()
+    clocks = ClockSampler(0).start()
     t_b, (Jb, ub) = timed(ens.run)
+    clock_info = clocks.stop()
     # fields are bit-identical across launch shapes; J sums per-block
     # partials, whose grouping follows the shape
     same = all(torch.equal(a, b) for a, b in zip(ub, us))
@@ -523,16 +535,53 @@ def run_ensemble(args):
             "sequential_cell_steps_per_s": cells / (t_s / 1e3), "speedup_vs_sequential": t_s / t_b,
             "solves_per_s_batched": len(members) / (t_b / 1e3),
             "solves_per_s_sequential": len(members) / (t_s / 1e3),
+            "speedup_vs_plain": t_s / t_b,
             "batched_ms": t_b, "sequential_ms": t_s, "fields_bitwise_equal_to_sequential": same, "J_max_rel_diff": j_rel,
             "members": len(members), "sizes": sizes, "steps": members[0].steps, "dtype": "f32",
+            "config": {"workload": "ensemble of 256 uneven solves", "sizes": "N in {64,128,256,512} w.p. "
+                       "{.4,.3,.2,.1}", "steps": members[0].steps, "dt": members[0].dt,
+                       "nu": "log-uniform [1e-4, 1e-2]", "theta": "within 20% of default, per solve",
+                       "plain": "256 sequential single-solve rollouts (single-solve tuned shapes)"},
+            "clocks": clock_info, "clocks_sequential": seq_clocks,
             "data": "synthetic", "chunk": 16}
+
+
+def plain_serve(reqs, dev, budget_s: float):
+    """The same requests solved one at a time through the plain per-request
+    API (a rollout, or a checkpointed adjoint gradient, per request; the
+    result read back before the next starts), in arrival order, for about
+    `budget_s` seconds: the throughput of serving without batching or
+    overlap."""
+    import torch
+    from ns_solver_jax_differential_distributed_gb300 import _native, serve
+    u0s = serve._U0Cache(dev)
+    n, t0 = 0, time.perf_counter()
+    for r in reqs:
+        if time.perf_counter() - t0 > budget_s:
+            break
+        u0 = u0s.get(r.N, r.seed)
+        th = torch.from_numpy(r.theta).to(dev)
+        if r.kind == "grad":
+            J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
+                                                  want_u_final=False, own_workspace=True)
+            float(J), g.cpu()
+        else:
+            J, u = _native.op_rollout(u0, th, r.steps, r.L, r.nu, r.dt, _native.SCHEME_IDS[r.scheme],
+                                      0.5, 0.1, 1.0, True)
+            float(J)
+        n += 1
+    wall = time.perf_counter() - t0
+    return {"solves": n, "wall_s": wall, "solves_per_s": n / wall}
 
 
 def run_serve(args):
     """Serving: Poisson arrivals at --rate for --duration s; N uniform over
     {128..2048}, steps U[100,2000], 30% forward+adjoint; 150 GB HBM budget;
     continuous batching.  Reports solves/s and p50/p99 latency; the run stops
-    30 s after the last arrival (requests still queued are reported)."""
+    30 s after the last arrival (requests still queued are reported).  The
+    same trace's requests, solved one by one through the plain per-request
+    API for about 30 s, give the plain throughput the served one is compared
+    with."""
     import torch
     from ns_solver_jax_differential_distributed_gb300 import _build, serve, autotune
     _build.build()
@@ -544,14 +593,27 @@ def run_serve(args):
     for N in (128, 256, 512, 1024, 2048):
         for s in range(16):
             srv.u0.get(N, s)
+    plain_serve(reqs[:8], dev, 5.0)  # warm-up: plans, workspaces, graphs
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(0).start()
     t0 = time.perf_counter()
     done, trace = srv.run(reqs, realtime=True, drain_limit=30.0)
     wall = time.perf_counter() - t0
+    clock_info = clocks.stop()
     summ = serve.summarize(reqs, done, wall)
+    clocks = ClockSampler(0).start()
+    plain = plain_serve(serve.make_trace(rate=args.rate, duration=args.duration, seed=7), dev, 30.0)
+    plain["clocks"] = clocks.stop()
     summ.update({"metric": "served solves/s", "rate_req_per_s": args.rate, "duration_s": args.duration,
                  "max_queue": max(q[1] for q in trace) if trace else 0,
                  "queue_at_end": trace[-1][1] if trace else 0,
-                 "grad_fraction_completed": sum(r.kind == "grad" for r in done) / max(1, len(done))})
+                 "grad_fraction_completed": sum(r.kind == "grad" for r in done) / max(1, len(done)),
+                 "plain_per_request": plain,
+                 "speedup_vs_plain": summ["solves_per_s"] / plain["solves_per_s"],
+                 "clocks": clock_info,
+                 "config": {"workload": "serving", "arrivals": f"Poisson {args.rate} req/s for {args.duration} s",
+                            "N": "uniform over {128,256,512,1024,2048}", "steps": "U[100,2000]",
+                            "grad_fraction": 0.3, "hbm_budget_bytes": 150e9, "dt": 1e-3}})
     return summ
 
 

@@ -15,6 +15,12 @@ time.  A scheduler thread owns the GPU:
   their kernels overlap the batched forward work on the device;
 * completion is detected with CUDA events; memory returns to the budget.
 
+Failures are isolated per request: every request ends with a ``status`` --
+"ok", "nonfinite" (its objective or gradient is not finite, e.g. a NaN in its
+initial state; NSGB_ERR_NONFINITE of the C ABI), "failed" (its allocation or
+its solve raised; ``error`` says why) or "cancelled" (``Server.cancel``) --
+and the others carry on with the same results as when served alone.
+
 Latency is measured from arrival to the moment the result (J, and dJ/dtheta
 for gradient requests) is on the host.  Results do not depend on what else
 is in flight: a request's arithmetic is that of a plain solve, which the
@@ -57,6 +63,9 @@ class Request:
     u_final: torch.Tensor = field(default=None, repr=False)
     t_admit: float = None
     t_done: float = None
+    status: str = None      # "ok", "nonfinite", "failed", "cancelled"
+    error: str = None
+    u0: torch.Tensor = field(default=None, repr=False)  # explicit initial state (else seeded)
 
     @property
     def cells(self) -> int:
@@ -67,12 +76,25 @@ class Request:
         return None if self.t_done is None else self.t_done - self.arrival
 
 
+# Time step of a request without an explicit one: the reference's stable step
+# (SimConfig.dt, NS_solver.py:75-79), min(cfl dx / v_max, dx^2 / (4 nu)) rounded
+# through float32, with its cfl of 0.4 and v_max = 4, a bound on the speed of
+# the seeded initial states (rms 1, maximum about 3).
+STABLE_CFL, STABLE_VMAX = 0.4, 4.0
+
+
+def stable_dt(N: int, L: float, nu: float) -> float:
+    dx = L / N
+    return float(np.float32(min(STABLE_CFL * dx / STABLE_VMAX, dx * dx / (4.0 * nu))))
+
+
 def make_trace(rate: float = 200.0, duration: float = 60.0, seed: int = 7,
                sizes=(128, 256, 512, 1024, 2048), steps_range=(100, 2000), p_grad: float = 0.3,
-               dt: float = 1e-3, nu_default: float = 1e-3):
+               dt: float = None, nu_default: float = 1e-3, scheme: str = "central"):
     """Poisson arrivals; N uniform over `sizes` (log-uniform over the
     power-of-two set), steps uniform in `steps_range`, gradient with
-    probability `p_grad`; theta seeded per request."""
+    probability `p_grad`; theta (and with it nu) seeded per request; dt the
+    stable step of each request's N and nu unless given."""
     rng = np.random.default_rng(seed)
     t, out = 0.0, []
     while True:
@@ -84,7 +106,9 @@ def make_trace(rate: float = 200.0, duration: float = 60.0, seed: int = 7,
         steps = int(rng.integers(steps_range[0], steps_range[1] + 1))
         kind = "grad" if rng.random() < p_grad else "forward"
         th = theta_draw(nu_default, seed=rid)
-        out.append(Request(rid, t, N, steps, kind, rid, nu=float(th[2]), dt=dt, theta=th))
+        nu = float(th[2])
+        step = stable_dt(N, TWO_PI, nu) if dt is None else dt
+        out.append(Request(rid, t, N, steps, kind, rid, nu=nu, dt=step, scheme=scheme, theta=th))
     return out
 
 
@@ -120,8 +144,29 @@ class Server:
         self.grad_workers = int(grad_workers)
         self.u0 = _U0Cache(self.device)
         self.used = 0.0
+        self.peak_used = 0.0
         self.stats = collections.Counter()
         self._lock = threading.Lock()
+        self._cancel = set()
+
+    def cancel(self, rid: int) -> None:
+        """Cancel request `rid`: dropped if still queued or advancing as a
+        forward solve (its memory returns to the budget at the next tick); a
+        gradient already running completes and is then reported cancelled."""
+        with self._lock:
+            self._cancel.add(int(rid))
+
+    def _cancelled(self, r: Request) -> bool:
+        with self._lock:
+            return r.rid in self._cancel
+
+    def _alloc(self, r: Request, shape, dtype) -> torch.Tensor:
+        """Device allocation of a request's resident fields (a test may
+        replace it to inject allocation failures)."""
+        return torch.empty(shape, dtype=dtype, device=self.device)
+
+    def _initial(self, r: Request) -> torch.Tensor:
+        return r.u0 if r.u0 is not None else self.u0.get(r.N, r.seed)
 
     # -- memory accounting
     def _fwd_bytes(self, r: Request) -> int:
@@ -144,7 +189,7 @@ class Server:
             r, nbytes = item
             try:
                 with torch.cuda.stream(stream):
-                    u0 = self.u0.get(r.N, r.seed)
+                    u0 = self._initial(r)
                     th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
                     J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
                                                           want_u_final=False, own_workspace=True)
@@ -154,7 +199,7 @@ class Server:
                 ev.synchronize()
                 r.J, r.grad = float(Jh), gh.numpy().copy()
                 done_q.put((r, nbytes, None))
-            except Exception as exc:  # handed to the scheduler, which raises it
+            except Exception as exc:  # this request fails; the worker serves on
                 done_q.put((r, nbytes, exc))
 
     def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None):
@@ -187,8 +232,14 @@ class Server:
                 nxt += 1
             # admission (FIFO): memory budget, and a cap on active forward work
             act_cells = sum(a["r"].N ** 2 for a in active)
+            while pending and self._cancelled(pending[0]):
+                r = pending.popleft()
+                r.status, r.t_done = "cancelled", time.perf_counter() - t0
+                completed.append(r)
             while pending:
                 r = pending[0]
+                if self._cancelled(r):
+                    break  # dropped at the top of the next pass
                 nb = self._grad_bytes(r) if r.kind == "grad" else self._fwd_bytes(r)
                 if self.used + nb > self.budget:
                     break
@@ -197,20 +248,40 @@ class Server:
                 if r.kind == "grad" and grads_inflight >= 2 * self.grad_workers:
                     break
                 pending.popleft()
-                self.used += nb
                 r.t_admit = time.perf_counter() - t0
                 if r.kind == "grad":
+                    self.used += nb
                     grads_inflight += 1
                     grad_q.put((r, nb))
                 else:
-                    plan = _native.get_plan(r.N, r.L, self.device)
-                    st_bytes = L.nsgb_rollout_workspace_bytes(plan.handle, r.steps)
-                    state = torch.empty(st_bytes, dtype=torch.uint8, device=self.device)
-                    out = torch.empty((2, r.N, r.N), dtype=torch.float32, device=self.device)
-                    Jt = torch.empty((), dtype=torch.float32, device=self.device)
-                    th = torch.from_numpy(r.theta).to(self.device)
+                    try:
+                        plan = _native.get_plan(r.N, r.L, self.device)
+                        st_bytes = L.nsgb_rollout_workspace_bytes(plan.handle, r.steps)
+                        state = self._alloc(r, (st_bytes,), torch.uint8)
+                        out = self._alloc(r, (2, r.N, r.N), torch.float32)
+                        Jt = self._alloc(r, (), torch.float32)
+                        th = torch.from_numpy(r.theta).to(self.device)
+                    except Exception as exc:  # this request fails; nothing was charged
+                        r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
+                        r.t_done = time.perf_counter() - t0
+                        completed.append(r)
+                        self.stats["failed"] += 1
+                        continue
+                    self.used += nb
                     active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=0, nb=nb, plan=plan))
                     act_cells += r.N ** 2
+                self.peak_used = max(self.peak_used, self.used)
+            # cancelled forward requests leave before the next tick
+            if active:
+                keep = []
+                for a in active:
+                    if self._cancelled(a["r"]):
+                        a["r"].status, a["r"].t_done = "cancelled", time.perf_counter() - t0
+                        self.used -= a["nb"]
+                        completed.append(a["r"])
+                    else:
+                        keep.append(a)
+                active = keep
             # one tick of continuous batching over the active forward requests
             if active:
                 arr = (_native.Member * len(active))()
@@ -218,7 +289,7 @@ class Server:
                     r = a["r"]
                     arr[k].plan = a["plan"].handle.value
                     arr[k].phys = _native.make_phys(r.L, r.nu, r.dt, r.scheme)
-                    arr[k].u0 = self.u0.get(r.N, r.seed).data_ptr()
+                    arr[k].u0 = self._initial(r).data_ptr()
                     arr[k].theta = a["th"].data_ptr()
                     arr[k].theta_len = a["th"].numel()
                     arr[k].u_final = a["out"].data_ptr()
@@ -256,6 +327,7 @@ class Server:
                     r = a["r"]
                     r.J = float(a["J"])
                     r.u_final = a["out"]
+                    r.status = "ok" if math.isfinite(r.J) else "nonfinite"
                     r.t_done = time.perf_counter() - t0
                     self.used -= a["nb"]
                     completed.append(r)
@@ -265,9 +337,13 @@ class Server:
             while not grad_done.empty():
                 r, nb, exc = grad_done.get()
                 if exc is not None:
-                    for _ in workers:
-                        grad_q.put(None)
-                    raise RuntimeError(f"gradient request {r.rid} (N={r.N}) failed") from exc
+                    r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
+                    self.stats["failed"] += 1
+                elif self._cancelled(r):
+                    r.status = "cancelled"
+                else:
+                    ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
+                    r.status = "ok" if ok else "nonfinite"
                 r.t_done = time.perf_counter() - t0
                 self.used -= nb
                 grads_inflight -= 1
@@ -287,11 +363,13 @@ class Server:
 
 
 def summarize(requests, completed, wall: float) -> dict:
-    lat = np.array([r.latency for r in completed if r.latency is not None])
-    cells = sum(r.cells * (3.5 if r.kind == "grad" else 1.0) for r in completed)
+    ok = [r for r in completed if r.status in (None, "ok")]
+    lat = np.array([r.latency for r in ok if r.latency is not None])
+    cells = sum(r.cells * (3.5 if r.kind == "grad" else 1.0) for r in ok)
+    statuses = collections.Counter(r.status or "ok" for r in completed)
     return {
-        "offered": len(requests), "completed": len(completed),
-        "solves_per_s": len(completed) / wall if wall > 0 else 0.0,
+        "offered": len(requests), "completed": len(ok), "statuses": dict(statuses),
+        "solves_per_s": len(ok) / wall if wall > 0 else 0.0,
         "p50_latency_s": float(np.percentile(lat, 50)) if lat.size else None,
         "p99_latency_s": float(np.percentile(lat, 99)) if lat.size else None,
         "forward_equiv_cell_steps_per_s": cells / wall if wall > 0 else 0.0,

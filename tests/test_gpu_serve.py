@@ -40,14 +40,65 @@ def test_mix_completes_and_equals_alone(serve):
 
 
 def test_admission_respects_budget(serve):
+    """A budget that holds only a few requests: every request still
+    completes, requests had to wait for memory, and the bytes in flight never
+    exceeded the budget."""
     reqs = _trace(serve, 16)
-    srv = serve.Server(hbm_budget=6e7, slice_steps=16, grad_workers=1)
-    peak = []
-    orig = srv.run
-
-    done, trace = orig(reqs, realtime=False)
-    assert len(done) == len(reqs)
+    srv = serve.Server(hbm_budget=1.0, slice_steps=16, grad_workers=1)
+    need = [srv._grad_bytes(r) if r.kind == "grad" else srv._fwd_bytes(r) for r in reqs]
+    srv.budget = budget = 1.5 * max(need)  # room for the largest request and a little more
+    assert budget < sum(need)
+    done, trace = srv.run(reqs, realtime=False)
+    assert len(done) == len(reqs) and all(r.status == "ok" for r in done)
+    assert 0 < srv.peak_used <= budget
+    assert max(t[1] for t in trace) > 0, "the budget never held a request back"
     assert srv.used == pytest.approx(0.0)
+
+
+def test_failures_are_isolated(serve):
+    """One request with a NaN in its initial state (status "nonfinite"), one
+    whose device allocation fails (status "failed") and one cancelled before it
+    runs: every other request completes with the bits of an undisturbed run."""
+    clean = _trace(serve, 30)
+    srv0 = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128, grad_workers=2)
+    ref, _ = srv0.run(clean, realtime=False)
+    ref = {r.rid: r for r in ref}
+
+    reqs = _trace(serve, 30)
+    fwd = [r for r in reqs if r.kind == "forward"]
+    grd = [r for r in reqs if r.kind == "grad"]
+    nan_f, nan_g, boom, gone = fwd[1], grd[0], fwd[3], fwd[5]
+    srv = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128, grad_workers=2)
+    for r in (nan_f, nan_g):
+        u0 = srv.u0.get(r.N, r.seed).clone()
+        u0[0, 2, 3] = float("nan")
+        r.u0 = u0
+    real_alloc = srv._alloc
+
+    def alloc(r, shape, dtype):
+        if r.rid == boom.rid:
+            raise torch.cuda.OutOfMemoryError("injected allocation failure")
+        return real_alloc(r, shape, dtype)
+
+    srv._alloc = alloc
+    srv.cancel(gone.rid)
+    done, _ = srv.run(reqs, realtime=False)
+    assert len(done) == len(reqs)
+    by = {r.rid: r for r in done}
+    assert by[nan_f.rid].status == "nonfinite" and by[nan_g.rid].status == "nonfinite"
+    assert by[boom.rid].status == "failed" and "injected" in by[boom.rid].error
+    assert by[gone.rid].status == "cancelled"
+    assert srv.used == pytest.approx(0.0)
+    for rid, r in by.items():
+        if rid in (nan_f.rid, nan_g.rid, boom.rid, gone.rid):
+            continue
+        assert r.status == "ok" and r.J == ref[rid].J, rid
+        if r.kind == "grad":
+            assert np.array_equal(r.grad, ref[rid].grad), rid
+        else:
+            assert torch.equal(r.u_final, ref[rid].u_final), rid
+    s = serve.summarize(reqs, done, 1.0)
+    assert s["statuses"] == {"ok": len(reqs) - 4, "nonfinite": 2, "failed": 1, "cancelled": 1}
 
 
 def test_summary(serve):
