@@ -526,6 +526,7 @@ def run_ensemble(args):
     # fields are bit-identical across launch shapes; J sums per-block
     # partials, whose grouping follows the shape
     same = all(torch.equal(a, b) for a, b in zip(ub, us))
+    finite = sum(bool(torch.isfinite(u).all()) and math.isfinite(float(j)) for u, j in zip(ub, Jb))
     j_rel = float(((Jb.double() - Js.double()).abs() / Js.double().abs().clamp_min(1e-30)).max())
     cells = float(ens.cell_steps)
     sizes = {}
@@ -535,7 +536,7 @@ def run_ensemble(args):
             "sequential_cell_steps_per_s": cells / (t_s / 1e3), "speedup_vs_sequential": t_s / t_b,
             "solves_per_s_batched": len(members) / (t_b / 1e3),
             "solves_per_s_sequential": len(members) / (t_s / 1e3),
-            "speedup_vs_plain": t_s / t_b,
+            "speedup_vs_plain": t_s / t_b, "finite_members": finite,
             "batched_ms": t_b, "sequential_ms": t_s, "fields_bitwise_equal_to_sequential": same, "J_max_rel_diff": j_rel,
             "members": len(members), "sizes": sizes, "steps": members[0].steps, "dtype": "f32",
             "config": {"workload": "ensemble of 256 uneven solves", "sizes": "N in {64,128,256,512} w.p. "

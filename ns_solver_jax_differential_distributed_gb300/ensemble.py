@@ -170,7 +170,8 @@ class Ensemble:
         return torch.stack(Js), us
 
 
-def from_workload(members, scheme: str = "central"):
-    """SolveSpecs from ``workloads.ensemble()`` members."""
-    return [SolveSpec(N=m.N, u0=m.u0(), theta=m.theta, nu=m.nu, dt=m.dt, scheme=scheme, L=m.L)
+def from_workload(members, scheme: str = None):
+    """SolveSpecs from ``workloads.ensemble()`` members (their own scheme
+    unless `scheme` is given)."""
+    return [SolveSpec(N=m.N, u0=m.u0(), theta=m.theta, nu=m.nu, dt=m.dt, scheme=scheme or m.scheme, L=m.L)
             for m in members]
