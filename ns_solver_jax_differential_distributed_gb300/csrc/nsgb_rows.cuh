@@ -43,6 +43,75 @@ __device__ __forceinline__ void cp_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory");
 }
 
+// ---- bulk copies: one thread moves whole row segments with the copy engine
+// (cp.async.bulk, completion counted in bytes on an mbarrier); every wait on
+// an mbarrier is bounded.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* mb, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb)), "r"(count) : "memory");
+}
+// make initialised mbarriers visible to the copy engine
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* mb, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)), "r"(bytes) : "memory");
+}
+// `bytes` (a multiple of 16, both addresses 16-byte aligned) from global src
+// to this CTA's shared dst; completes `bytes` transactions on mb.
+__device__ __forceinline__ void bulk_g2s(float* dst, const float* src, unsigned bytes, uint64_t* mb, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mb)), "l"(pol)
+      : "memory");
+}
+// Wait for the phase of parity `parity` of mb to complete, polling at most
+// `limit` times; false if it did not.
+__device__ __forceinline__ bool mbar_wait(uint64_t* mb, unsigned parity, unsigned limit) {
+  const uint32_t a = smem_u32(mb);
+  for (unsigned i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Segments of one band row as bulk copies: ring offset, source column and
+// length in floats; the W + 8 columns from j0 - 4 (W < N), or the row with
+// four wrapped columns at each end (W = N), split where the periodic wrap
+// falls.  All offsets and lengths are multiples of four floats (16 bytes).
+struct RowPieces {
+  int n;
+  int dst[3], col[3], len[3];
+};
+__device__ __forceinline__ RowPieces row_pieces(int N, int W, int j0) {
+  RowPieces r;
+  if (W == N) {
+    r.n = 3;
+    r.dst[0] = 4, r.col[0] = N - 4, r.len[0] = 4;
+    r.dst[1] = 8, r.col[1] = 0, r.len[1] = N;
+    r.dst[2] = N + 8, r.col[2] = 0, r.len[2] = 4;
+  } else if (j0 == 0) {
+    r.n = 2;
+    r.dst[0] = 4, r.col[0] = N - 4, r.len[0] = 4;
+    r.dst[1] = 8, r.col[1] = 0, r.len[1] = W + 4;
+  } else if (j0 + W == N) {
+    r.n = 2;
+    r.dst[0] = 4, r.col[0] = j0 - 4, r.len[0] = W + 4;
+    r.dst[1] = W + 8, r.col[1] = 0, r.len[1] = 4;
+  } else {
+    r.n = 1;
+    r.dst[0] = 4, r.col[0] = j0 - 4, r.len[0] = W + 8;
+  }
+  return r;
+}
+
 __device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
   *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
 }

@@ -208,10 +208,15 @@ __global__ void __launch_bounds__(256) k_stencil_batch(const SolveDev* __restric
 //     values of u(t-1) of the neighbouring groups,
 //   - writes u*next(t-2) and rhs(t-2) = div(u*next)/dt, and adds the row's
 //     objective partial u_x(t-2) f_x.
-// The input rows (p and u*) arrive in shared-memory rings by per-thread
-// asynchronous copies issued kAhead rows ahead, so the loads of later rows
-// overlap the arithmetic without holding registers; p neighbours come straight
-// from the ring.  Computed values that other groups need (the first and last
+// The input rows (p and u*) arrive in shared-memory rings kAhead rows ahead,
+// so the loads of later rows overlap the arithmetic without holding
+// registers; p neighbours come straight from the ring.  The copies are either
+// per-thread 16-byte asynchronous copies (each thread its own columns) or,
+// with BULK, a few bulk copies of whole row segments issued by one thread
+// through the copy engine, counted on an mbarrier per group of rows: thread 0
+// waits for the next group before the iteration's barrier, bounded; if a
+// wait runs out the CTA stops marching, drains its copies in flight and
+// writes a NaN objective partial, so the call's J comes out non-finite.  Computed values that other groups need (the first and last
 // column of a group of u and u*next_y) pass through small edge arrays,
 // double-buffered by iteration parity; one barrier per iteration orders
 // both.  The i-neighbours of computed rows never leave registers.
@@ -221,17 +226,30 @@ constexpr int F_UX = 0, F_UY = 1, F_SY = 2;  // exchanged fields
 constexpr int kAhead = 3;                    // rows copied ahead of use
 constexpr int kPRing = 8;                    // p rows t-1 .. t+1+kAhead (power of two)
 constexpr int kURing = 4;                    // u* rows t .. t+kAhead (power of two)
-static_assert(kPRing >= kAhead + 3 && kURing >= kAhead + 1, "ring depth");
+constexpr int kMbSlots = 4;                  // mbarriers of row groups in flight (power of two)
+static_assert(kPRing >= kAhead + 3 && kURing >= kAhead + 1 && kMbSlots >= kAhead + 1, "ring depth");
+
+constexpr unsigned kWaitLimit = 1u << 22;  // mbarrier polls before a CTA gives up
+// Row copies by the copy engine (BULK) or per thread.  Measured at N=4096
+// (band 2048 x 54, in the pipelined step): 84.3 us per launch with bulk
+// copies at prefetch depth 3 or 5, 72.6 us with per-thread copies -- thread
+// 0's issuing and polling lies on every iteration's barrier -- so the kernels
+// use per-thread copies; both give the same bits.
+constexpr bool kBulkRows = false;
 
 // shared memory: rings, edges [2 slots][3 fields][2 sides][G], forcing rows,
-// 32 partial sums
+// 32 partial sums, then (8-byte aligned) kMbSlots + 1 mbarriers
+inline size_t floats_before_mbar(int N, int W, int RH) {
+  const size_t f = (size_t)(kPRing + 2 * kURing) * ring_stride(W) + (size_t)12 * groups(N, W) + RH + 2 + 32;
+  return (f + 1) & ~(size_t)1;
+}
 inline size_t smem_bytes(int N, int W, int RH) {
-  return sizeof(float) * ((size_t)(kPRing + 2 * kURing) * ring_stride(W) + (size_t)12 * groups(N, W) + RH + 2 + 32);
+  return sizeof(float) * floats_before_mbar(N, W, RH) + (kMbSlots + 1) * sizeof(uint64_t);
 }
 
 }  // namespace rows
 
-template <int SCHEME>
+template <int SCHEME, bool BULK>
 __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step_off) {
   using namespace rows;
   const StepConsts& c = a.c;
@@ -262,6 +280,10 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   float* sF = sE + 12 * G;                     // f_x of rows r0-1 .. r1
   float* sRed = sF + RH + 2;                   // per-warp partial sums
   auto edge = [&](int slot, int f, int side) { return sE + ((slot * 3 + f) * 2 + side) * G; };
+  // mbarriers (BULK): [0, kMbSlots) the groups of iterations t (p row t+1,
+  // u* row t) by (t - r0 + 2) mod kMbSlots, [kMbSlots] the prologue's p rows
+  // r0-3, r0-2
+  uint64_t* sMb = reinterpret_cast<uint64_t*>(sm + (((kPRing + 2 * kURing) * (size_t)RS + (size_t)12 * G + RH + 2 + 32 + 1) & ~(size_t)1));
 
   int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
   const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
@@ -278,6 +300,22 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   const float* __restrict__ usy_g = a.us + NN;
   // one copy group: p row `pr` (if do_p) and u* row `ur` (if do_u)
   const uint64_t pol = evict_first_policy();
+  const RowPieces pcs = row_pieces(N, W, j0);
+  const unsigned row_bytes = 4u * (unsigned)(W + 8);
+  auto issue_bulk = [&](int pr, bool do_p, int ur, bool do_u, uint64_t* mb) {  // thread 0
+    const bool cp_p = do_p && has_p;
+    mbar_expect_tx(mb, row_bytes * ((cp_p ? 1u : 0u) + (do_u ? 2u : 0u)));
+    for (int k = 0; k < pcs.n; ++k) {
+      const unsigned nb = 4u * (unsigned)pcs.len[k];
+      if (cp_p) bulk_g2s(sP + (pr & (kPRing - 1)) * RS + pcs.dst[k], pp + (size_t)(pr & M) * N + pcs.col[k], nb, mb, pol);
+      if (do_u) {
+        const size_t o = (size_t)(ur & M) * N + pcs.col[k];
+        const int d = (ur & (kURing - 1)) * RS + pcs.dst[k];
+        bulk_g2s(sUX + d, usx_g + o, nb, mb, pol);
+        bulk_g2s(sUY + d, usy_g + o, nb, mb, pol);
+      }
+    }
+  };
   auto issue = [=](int pr, bool do_p, int ur, bool do_u) {
     if (do_p && has_p) {
       float* dst = sP + (pr & (kPRing - 1)) * RS;
@@ -296,12 +334,35 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   };
   // prologue: p rows r0-3, r0-2, then the groups of iterations r0-2-kAhead ..
   // r0-3 (p rows r0-1 .., u* rows r0-2 ..); wait for those of iteration r0-2
-  issue(r0 - 3, true, 0, false);
-  issue(r0 - 2, true, 0, false);
+  auto mb_of = [&](int t) { return sMb + ((t - r0 + 2) & (kMbSlots - 1)); };  // group of iteration t
+  auto par_of = [&](int t) { return (unsigned)(((t - r0 + 2) / kMbSlots) & 1); };
+  uint64_t* mb_pro = sMb + kMbSlots;
+  int issued = min(r0 - 2 + kAhead - 1, r1 + 1);  // last iteration whose group was issued (BULK)
+  int waited = r0 - 2;               // last iteration whose group was waited for (BULK)
+  bool late = false;  // thread 0: a wait ran out (BULK)
+  if constexpr (BULK) {
+    if (tid == 0) {
+      for (int k = 0; k <= kMbSlots; ++k) mbar_init(sMb + k, 1);
+      mbar_init_fence();
+      // the prologue's two p rows share one mbarrier
+      mbar_expect_tx(mb_pro, has_p ? 2u * row_bytes : 0u);
+      if (has_p)
+        for (int r = r0 - 3; r <= r0 - 2; ++r)
+          for (int k = 0; k < pcs.n; ++k)
+            bulk_g2s(sP + (r & (kPRing - 1)) * RS + pcs.dst[k], pp + (size_t)(r & M) * N + pcs.col[k],
+                     4u * (unsigned)pcs.len[k], mb_pro, pol);
+      for (int t = r0 - 2; t <= issued; ++t) issue_bulk(t + 1, true, t, true, mb_of(t));
+      late = !mbar_wait(mb_pro, 0, kWaitLimit) || !mbar_wait(mb_of(r0 - 2), 0, kWaitLimit);
+    }
+  } else {
+    issue(r0 - 3, true, 0, false);
+    issue(r0 - 2, true, 0, false);
 #pragma unroll
-  for (int k = kAhead; k >= 1; --k) issue(r0 - 1 - k + kAhead, true, r0 - 2 - k + kAhead, true);
-  cp_wait<kAhead - 1>();
-  __syncthreads();
+    for (int k = kAhead; k >= 1; --k) issue(r0 - 1 - k + kAhead, true, r0 - 2 - k + kAhead, true);
+    cp_wait<kAhead - 1>();
+  }
+  // the barrier also tells every thread whether thread 0 gave up waiting
+  bool aborted = __syncthreads_or(late) != 0;
 
   // registers entering iteration t: u rows t-1, t-2; u*next x rows t-3, t-2
   // and y row t-2
@@ -312,9 +373,17 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   float* __restrict__ uso_y = a.us_out + NN;
   float* __restrict__ rhs_g = a.rhs;
 #pragma unroll 1
-  for (int t = r0 - 2; t <= r1 + 1; ++t) {
+  for (int t = r0 - 2; t <= r1 + 1 && !aborted; ++t) {
     const int rs = (t - 1) & 1, ws = t & 1;
-    issue(t + 1 + kAhead, true, t + kAhead, true);
+    if constexpr (BULK) {
+      // rows beyond the band's last iteration are never read: not copied
+      if (tid == 0 && t + kAhead <= r1 + 1) {
+        issue_bulk(t + 1 + kAhead, true, t + kAhead, true, mb_of(t + kAhead));
+        issued = t + kAhead;
+      }
+    } else {
+      issue(t + 1 + kAhead, true, t + kAhead, true);
+    }
 
     // u(t): projection of row t
     float ux[4], uy[4];
@@ -391,10 +460,27 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
       sx2[k] = sx1[k];
       sy2[k] = sy1[k];
     }
-    cp_wait<kAhead - 1>();  // the rows of iteration t+1 have landed
-    __syncthreads();
+    if constexpr (BULK) {
+      if (tid == 0 && t + 1 <= r1 + 1) {  // the rows of iteration t+1 have landed
+        late = !mbar_wait(mb_of(t + 1), par_of(t + 1), kWaitLimit);
+        waited = t + 1;
+      }
+      aborted = __syncthreads_or(late) != 0;
+    } else {
+      cp_wait<kAhead - 1>();  // the rows of iteration t+1 have landed
+      __syncthreads();
+    }
   }
-  cp_wait<0>();
+  if constexpr (BULK) {
+    // no copy may still be writing into this CTA's shared memory when it
+    // exits: wait (bounded again) for every group not yet seen complete
+    if (tid == 0) {
+      if (aborted) (void)mbar_wait(mb_pro, 0, kWaitLimit);
+      for (int t = aborted ? waited : waited + 1; t <= issued; ++t) (void)mbar_wait(mb_of(t), par_of(t), kWaitLimit);
+    }
+  } else {
+    cp_wait<0>();
+  }
 
   // objective partial of the CTA
   jacc = warp_sum(jacc);
@@ -404,6 +490,7 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   if (warp == 0) {
     float v = lane < nwarps ? sRed[lane] : 0.0f;
     v = warp_sum(v);
+    if (aborted) v = __int_as_float(0x7fc00000);  // NaN: the step did not complete
     if (lane == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
       const int nblk = gridDim.x * gridDim.y;
       a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
@@ -413,13 +500,13 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
 
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows(const StencilArgs a) {
-  stencil_rows_body<SCHEME>(a, 0);
+  stencil_rows_body<SCHEME, rows::kBulkRows>(a, 0);
 }
 
 template <int SCHEME>
 __global__ void __launch_bounds__(544, 1) k_stencil_rows_batch(const SolveDev* __restrict__ solves, int variant,
                                                               int step_off) {
-  stencil_rows_body<SCHEME>(solves[blockIdx.z].st[variant], step_off);
+  stencil_rows_body<SCHEME, rows::kBulkRows>(solves[blockIdx.z].st[variant], step_off);
 }
 
 bool stencil_rows_mode(int tw) { return tw >= NSGB_ROWS_MIN_W; }
