@@ -13,7 +13,8 @@ It launches few kernels, so it is the command to capture under ncu.
     python -m ns_solver_jax_differential_distributed_gb300.profile_stages --N 4096 --scheme upwind --adjoint 6
 
 times the backward steps of a 6-step gradient (adjoint stencil and FFT passes
-per step, every state stored) instead.
+per step, every state stored) instead; ``--fused -1`` times the two kernels of
+the fused-row step (nsgb_plan_set_fused) instead of the four.
 """
 from __future__ import annotations
 
@@ -146,6 +147,9 @@ def main(argv=None):
     ap.add_argument("--adjoint-tiles", default="", help="tw,th of the adjoint stencil")
     ap.add_argument("--tuned", action="store_true",
                     help="apply the autotuner's cached shapes for (N, scheme) first (as bench.py runs them)")
+    ap.add_argument("--fused", type=int, default=0, metavar="ROWS",
+                    help="time the two-kernel step with the fused row kernel (bands of ROWS rows; -1: the "
+                         "band that fits every cluster at once)")
     args = ap.parse_args(argv)
     _build.build()
     dev = torch.device("cuda")
@@ -163,6 +167,7 @@ def main(argv=None):
         plan.set_tiles(*[int(x) for x in args.tiles.split(",")])
     if args.adjoint_tiles:
         plan.set_adjoint_tiles(*[int(x) for x in args.adjoint_tiles.split(",")])
+    plan.set_fused(args.fused)
     if args.adjoint:
         # forward once, then `reps` backward phases (adjoint stencil + FFT
         # passes per step), timed with CUDA events; few launches, so the
@@ -191,7 +196,8 @@ def main(argv=None):
             peak = float(json.load(f)["hbm_gbs"])
     except Exception:
         peak = 6800.0
-    out = {"N": args.N, "scheme": args.scheme, "tiles": plan.tiles(), "radix": plan.fft_radix(), "stages": {}}
+    out = {"N": args.N, "scheme": args.scheme, "tiles": plan.tiles(), "radix": plan.fft_radix(),
+           "fused_rows": plan.fused_rows(), "stages": {}}
     for k, ms in st.items():
         gbs = _native.STAGE_BYTES_PER_CELL[k] * args.N * args.N / (ms * 1e-3) / 1e9
         out["stages"][k] = {"ms": round(ms, 5), "GB/s": round(gbs, 1), "frac": round(gbs / peak, 3)}
