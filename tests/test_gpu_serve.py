@@ -29,7 +29,8 @@ def test_mix_completes_and_equals_alone(serve):
     assert max(t[2] for t in trace) > 1, "requests were never batched together"
     picks = [r for r in reqs if r.kind == "forward"][:3] + [r for r in reqs if r.kind == "grad"][:2]
     for r in picks:
-        alone = serve.Request(r.rid, 0.0, r.N, r.steps, r.kind, r.seed, nu=r.nu, dt=r.dt, theta=r.theta)
+        alone = serve.Request(r.rid, 0.0, r.N, r.steps, r.kind, r.seed, nu=r.nu, dt=r.dt, scheme=r.scheme,
+                              theta=r.theta)
         srv1 = serve.Server(hbm_budget=2e9, slice_steps=5, grad_workers=1)
         (a,), _ = srv1.run([alone], realtime=False)
         assert a.J == r.J, (r.rid, a.J, r.J)
