@@ -45,3 +45,27 @@ def test_optimizer_specs():
     assert r.kind == _native.OPT_RMSPROP and r.decay == pytest.approx(0.9) and r.eps == pytest.approx(1e-8)
     with pytest.raises(ValueError):
         optimization.OptimizerSpec("lamb", 0.1).native()
+
+
+def test_trace_time_step_is_the_reference_stable_step():
+    """Each request's dt is SimConfig.dt's rule (NS_solver.py:75-79) for its N
+    and nu, rounded through float32, with upwind advection by default."""
+    reqs = serve.make_trace(rate=100.0, duration=1.0, seed=5)
+    for r in reqs:
+        dx = 2 * np.pi / r.N
+        expect = float(np.float32(min(0.4 * dx / 4.0, dx * dx / (4 * r.nu))))
+        assert r.dt == expect == serve.stable_dt(r.N, 2 * np.pi, r.nu)
+        assert r.scheme == "upwind"
+    fixed = serve.make_trace(rate=100.0, duration=0.2, seed=5, dt=1e-3, scheme="central")
+    assert all(r.dt == 1e-3 and r.scheme == "central" for r in fixed)
+
+
+def test_summarize_counts_only_ok_results():
+    reqs = serve.make_trace(rate=100.0, duration=0.5, seed=4, sizes=(64,), steps_range=(10, 10), p_grad=0.0)
+    for i, r in enumerate(reqs):
+        r.t_done = r.arrival + 0.1
+        r.status = ["ok", "nonfinite", "failed", "cancelled"][i % 4]
+    s = serve.summarize(reqs, reqs, wall=1.0)
+    n_ok = sum(r.status == "ok" for r in reqs)
+    assert s["completed"] == n_ok and s["solves_per_s"] == pytest.approx(n_ok)
+    assert sum(s["statuses"].values()) == len(reqs) and s["statuses"]["ok"] == n_ok
