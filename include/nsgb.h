@@ -200,6 +200,48 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
                       float* J, float* u_final, float* dJdtheta, float* dJdu0, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* One gradient solve of a batch advanced by nsgb_grad_batch_advance. */
+typedef struct nsgb_grad_member {
+  const nsgb_plan* plan; /* plan of this solve's N and L; its launch shapes must not
+                            change while the solve is in progress */
+  nsgb_phys phys;
+  const float* u0;       /* (2,N,N) device */
+  const float* theta;    /* device, theta_len entries */
+  int theta_len;
+  int steps, every;      /* rollout length and checkpoint interval */
+  float* J;              /* one float, device; written when the forward phase ends */
+  float* u_final;        /* (2,N,N) device or NULL; written with J */
+  float* dJdtheta;       /* device, theta_len entries; written when the solve completes */
+  float* dJdu0;          /* (2,N,N) device or NULL; written when the solve completes */
+  void* state;           /* device state kept between calls:
+                            nsgb_rollout_grad_workspace_bytes(plan, steps, every) bytes,
+                            256-byte aligned */
+  int done_ops;          /* operations of its schedule already done (0: not started) */
+} nsgb_grad_member;
+
+/* Operations in the schedule of one gradient solve (0 on invalid arguments):
+ * `steps` forward steps, then per checkpoint segment (last first) its
+ * recomputed steps and its `steps`-many adjoint steps in total. */
+int nsgb_grad_ops(int steps, int every);
+
+/* Bytes of workspace for nsgb_grad_batch_advance of `count` solves by up to
+ * `ops` operations (the argument tables of the call). */
+size_t nsgb_grad_batch_workspace_bytes(int count, int ops);
+
+/* Batched, continuously batchable form of nsgb_rollout_grad (both phases;
+ * jax.grad of the rollout objective, NS_solver.py:725): every member performs
+ * min(ops, nsgb_grad_ops(steps, every) - done_ops) further operations of its
+ * schedule, the members in lock-step.  At each step, the stencils of the
+ * forward and recomputed steps of all members with the same plan and scheme
+ * are ONE batched launch, their adjoint stencils another, and all their
+ * FFT-Poisson solves one batched launch per pass.  Each member's J, u_final,
+ * dJdtheta and dJdu0 equal those of nsgb_rollout_grad with the same
+ * arguments bit for bit, however its work is split into calls and whatever
+ * else is in the batch.  The caller advances done_ops itself.  Uploads its
+ * argument tables from host memory, so it refuses a capturing stream. */
+int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
 /* One member of an ensemble of independent solves (see nsgb_ensemble_advance). */
 typedef struct nsgb_member {
   const nsgb_plan* plan; /* plan of this member's N and L (tiles as tuned) */

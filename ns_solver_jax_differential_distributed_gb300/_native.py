@@ -39,6 +39,15 @@ class Member(ctypes.Structure):
                 ("done_steps", ctypes.c_int)]
 
 
+class GradMember(ctypes.Structure):
+    """``nsgb_grad_member`` (include/nsgb.h): one solve of a gradient batch."""
+    _fields_ = [("plan", ctypes.c_void_p), ("phys", Phys), ("u0", ctypes.c_void_p),
+                ("theta", ctypes.c_void_p), ("theta_len", ctypes.c_int), ("steps", ctypes.c_int),
+                ("every", ctypes.c_int), ("J", ctypes.c_void_p), ("u_final", ctypes.c_void_p),
+                ("dJdtheta", ctypes.c_void_p), ("dJdu0", ctypes.c_void_p), ("state", ctypes.c_void_p),
+                ("done_ops", ctypes.c_int)]
+
+
 class Optimizer(ctypes.Structure):
     """``nsgb_optimizer`` (include/nsgb.h)."""
     _fields_ = [("kind", ctypes.c_int), ("learning_rate", ctypes.c_double), ("b1", ctypes.c_double),
@@ -97,6 +106,9 @@ SIGNATURES = {
     "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_poisson_noalloc": ([_I, _D, _P, _P, _P], _I),
+    "nsgb_grad_ops": ([_I, _I], _I),
+    "nsgb_grad_batch_workspace_bytes": ([_I, _I], _S),
+    "nsgb_grad_batch_advance": ([ctypes.POINTER(GradMember), _I, _I, _P, _S, _P], _I),
     "nsgb_optimize_workspace_bytes": ([_P, _I, _I, _I], _S),
     "nsgb_optimize": ([_P, _PH, _P, _P, _I, _I, _I, ctypes.POINTER(Optimizer), _I, _P, _P, _P, _S, _P], _I),
 }

@@ -112,7 +112,7 @@ __device__ __forceinline__ void forcing_theta_grad(int i, const ForcingRow& fr, 
 }
 
 template <int SCHEME, int TW, int TH>
-__global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
+__device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
   using Lay = AdjointSmem<TW, TH>;
   constexpr int G = Lay::G, W4 = Lay::W4, PH = Lay::PH, UH = Lay::UH, SH = Lay::SH, SW = Lay::SW;
   extern __shared__ __align__(16) float sm[];
@@ -257,18 +257,33 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
 }
 
 template <int SCHEME, int TW, int TH>
-static cudaError_t launch_adjoint_t(const AdjointArgs& a, cudaStream_t st) {
-  const cudaError_t e = raise_smem_limit(k_adjoint<SCHEME, TW, TH>);
+__global__ void __launch_bounds__(256) k_adjoint(const AdjointArgs a) {
+  adjoint_body<SCHEME, TW, TH>(a);
+}
+// Batched form: blockIdx.z selects the solve's arguments.
+template <int SCHEME, int TW, int TH>
+__global__ void __launch_bounds__(256) k_adjoint_b(const AdjointArgs* __restrict__ tab) {
+  adjoint_body<SCHEME, TW, TH>(tab[blockIdx.z]);
+}
+
+// a: the shape, scheme and N of the launch; tab (device, count entries) or
+// nullptr for the single launch with a itself.
+template <int SCHEME, int TW, int TH>
+static cudaError_t launch_adjoint_t(const AdjointArgs& a, const AdjointArgs* tab, int count, cudaStream_t st) {
+  const cudaError_t e = tab ? raise_smem_limit(k_adjoint_b<SCHEME, TW, TH>) : raise_smem_limit(k_adjoint<SCHEME, TW, TH>);
   if (e != cudaSuccess) return e;
-  const dim3 grid(a.c.N / TW, a.c.N / TH);
-  k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), AdjointSmem<TW, TH>::BYTES, st>>>(a);
+  const dim3 grid(a.c.N / TW, a.c.N / TH, tab ? count : 1);
+  if (tab)
+    k_adjoint_b<SCHEME, TW, TH><<<grid, dim3(32, 8), AdjointSmem<TW, TH>::BYTES, st>>>(tab);
+  else
+    k_adjoint<SCHEME, TW, TH><<<grid, dim3(32, 8), AdjointSmem<TW, TH>::BYTES, st>>>(a);
   return cudaGetLastError();
 }
 
 template <int SCHEME>
-static cudaError_t launch_adjoint_s(const AdjointArgs& a, cudaStream_t st) {
+static cudaError_t launch_adjoint_s(const AdjointArgs& a, const AdjointArgs* tab, int count, cudaStream_t st) {
 #define NSGB_TILE_CASE(W, H) \
-  if (a.tw == W && a.th == H) return launch_adjoint_t<SCHEME, W, H>(a, st);
+  if (a.tw == W && a.th == H) return launch_adjoint_t<SCHEME, W, H>(a, tab, count, st);
   NSGB_STENCIL_TILES(NSGB_TILE_CASE)
 #undef NSGB_TILE_CASE
   return cudaErrorInvalidValue;
@@ -303,7 +318,7 @@ inline size_t smem_bytes(int N, int W, int RH) {
 }  // namespace adjrows
 
 template <int SCHEME>
-__global__ void __launch_bounds__(NSGB_ADJ_ROWS_MAX_W / 4 + 32) k_adjoint_rows(const AdjointArgs a) {
+__device__ __forceinline__ void adjoint_rows_body(const AdjointArgs& a) {
   using namespace rows;
   using adjrows::kAhead;
   using adjrows::kLRing;
@@ -526,31 +541,52 @@ __global__ void __launch_bounds__(NSGB_ADJ_ROWS_MAX_W / 4 + 32) k_adjoint_rows(c
   }
 }
 
+template <int SCHEME>
+__global__ void __launch_bounds__(NSGB_ADJ_ROWS_MAX_W / 4 + 32) k_adjoint_rows(const AdjointArgs a) {
+  adjoint_rows_body<SCHEME>(a);
+}
+template <int SCHEME>
+__global__ void __launch_bounds__(NSGB_ADJ_ROWS_MAX_W / 4 + 32) k_adjoint_rows_b(const AdjointArgs* __restrict__ tab) {
+  adjoint_rows_body<SCHEME>(tab[blockIdx.z]);
+}
+
 bool adjoint_rows_supported(int N, int tw, int th) {
   if (!stencil_rows_mode(tw) || (tw & (tw - 1)) != 0 || tw > NSGB_ADJ_ROWS_MAX_W) return false;
   return th >= 1 && th <= N && adjrows::smem_bytes(N, rows::band_width(N, tw), th) <= 227 * 1024;
 }
 
 template <int SCHEME>
-static cudaError_t launch_adjoint_rows(const AdjointArgs& a, cudaStream_t st) {
+static cudaError_t launch_adjoint_rows(const AdjointArgs& a, const AdjointArgs* tab, int count, cudaStream_t st) {
   const int N = a.c.N;
   const int W = rows::band_width(N, a.tw);
   const size_t smem = adjrows::smem_bytes(N, W, a.th);
   if (smem > 48 * 1024) {
-    const cudaError_t e = raise_smem_limit(k_adjoint_rows<SCHEME>);
+    const cudaError_t e = tab ? raise_smem_limit(k_adjoint_rows_b<SCHEME>) : raise_smem_limit(k_adjoint_rows<SCHEME>);
     if (e != cudaSuccess) return e;
   }
-  const dim3 grid(N / W, (N + a.th - 1) / a.th);
-  k_adjoint_rows<SCHEME><<<grid, rows::threads(N, W), smem, st>>>(a);
+  const dim3 grid(N / W, (N + a.th - 1) / a.th, tab ? count : 1);
+  if (tab)
+    k_adjoint_rows_b<SCHEME><<<grid, rows::threads(N, W), smem, st>>>(tab);
+  else
+    k_adjoint_rows<SCHEME><<<grid, rows::threads(N, W), smem, st>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
+static cudaError_t launch_adjoint_any(const AdjointArgs& a, const AdjointArgs* tab, int count, cudaStream_t st) {
   if (stencil_rows_mode(a.tw))
-    return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_rows<NSGB_SCHEME_CENTRAL>(a, st)
-                                           : launch_adjoint_rows<NSGB_SCHEME_UPWIND>(a, st);
-  return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_s<NSGB_SCHEME_CENTRAL>(a, st)
-                                         : launch_adjoint_s<NSGB_SCHEME_UPWIND>(a, st);
+    return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_rows<NSGB_SCHEME_CENTRAL>(a, tab, count, st)
+                                           : launch_adjoint_rows<NSGB_SCHEME_UPWIND>(a, tab, count, st);
+  return a.scheme == NSGB_SCHEME_CENTRAL ? launch_adjoint_s<NSGB_SCHEME_CENTRAL>(a, tab, count, st)
+                                         : launch_adjoint_s<NSGB_SCHEME_UPWIND>(a, tab, count, st);
+}
+
+cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st) {
+  return launch_adjoint_any(a, nullptr, 1, st);
+}
+
+cudaError_t launch_adjoint_batch(const AdjointArgs& shape, const AdjointArgs* tab, int count, cudaStream_t st) {
+  if (!tab || count < 1) return cudaErrorInvalidValue;
+  return launch_adjoint_any(shape, tab, count, st);
 }
 
 // Fixed-order reduction of nrows x nblk x 3 partials into gacc[3] (double):

@@ -1227,6 +1227,359 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   return NSGB_OK;
 }
 
+}  // extern "C"
+
+// --------------------------------------------------- batched gradients --
+namespace {
+enum { GOP_FWD = 0, GOP_REC = 1, GOP_ADJ = 2 };
+// One operation of a gradient solve: a forward step (with its checkpoint), a
+// recomputed step of checkpoint segment [s0, s1), or an adjoint step.
+struct GradOp {
+  int kind;
+  int s;        // step index
+  int seg, s0, s1;
+};
+inline int grad_seg_ops(int len) { return len == 1 ? 1 : 2 * len; }
+
+// The operations in the order grad_enqueue issues them: `steps` forward steps,
+// then per checkpoint segment, last first, its recomputed steps (none for a
+// one-step segment, whose state is its checkpoint) and its adjoint steps.
+int grad_ops_total(int steps, int every) {
+  const int nseg = (steps + every - 1) / every;
+  const int last = steps - (nseg - 1) * every;
+  return steps + grad_seg_ops(last) + (nseg - 1) * grad_seg_ops(every);
+}
+
+GradOp grad_op(int steps, int every, int k) {
+  GradOp o{};
+  if (k < steps) {
+    o.kind = GOP_FWD;
+    o.s = k;
+    return o;
+  }
+  int r = k - steps;
+  const int nseg = (steps + every - 1) / every;
+  const int last = steps - (nseg - 1) * every;
+  if (r < grad_seg_ops(last)) {
+    o.seg = nseg - 1;
+  } else {
+    r -= grad_seg_ops(last);
+    const int q = r / grad_seg_ops(every);
+    r -= q * grad_seg_ops(every);
+    o.seg = nseg - 2 - q;
+  }
+  o.s0 = o.seg * every;
+  o.s1 = std::min(steps, o.s0 + every);
+  const int len = o.s1 - o.s0;
+  if (len > 1 && r < len) {
+    o.kind = GOP_REC;
+    o.s = o.s0 + r;
+  } else {
+    o.kind = GOP_ADJ;
+    o.s = o.s1 - 1 - (r - (len > 1 ? len : 0));
+  }
+  return o;
+}
+
+int check_grad_members(const nsgb_grad_member* m, int count) {
+  if (!m || count <= 0) return fail(NSGB_ERR_INVALID_ARG, "empty gradient batch");
+  for (int i = 0; i < count; ++i) {
+    const nsgb_grad_member& x = m[i];
+    if (!x.plan) return fail(NSGB_ERR_INVALID_ARG, "member %d: plan is NULL", i);
+    if (int r = check_phys(&x.phys)) return r;
+    if (std::fabs(x.phys.L - x.plan->L) > 1e-12 * x.plan->L)
+      return fail(NSGB_ERR_INVALID_ARG, "member %d: phys.L differs from its plan's L", i);
+    if (int r = check_theta(x.theta, x.theta_len)) return r;
+    if (int r = check_field(x.u0, "member u0")) return r;
+    if (!x.J || !x.dJdtheta) return fail(NSGB_ERR_INVALID_ARG, "member %d: J or dJdtheta is NULL", i);
+    if (x.steps < 1 || x.every < 1)
+      return fail(NSGB_ERR_INVALID_ARG, "member %d: steps and every must be >= 1", i);
+    if (!x.state || ((uintptr_t)x.state & 255))
+      return fail(NSGB_ERR_WORKSPACE, "member %d: state must be non-NULL and 256-byte aligned", i);
+    if (x.done_ops < 0 || x.done_ops > grad_ops_total(x.steps, x.every))
+      return fail(NSGB_ERR_INVALID_ARG, "member %d: done_ops out of range", i);
+  }
+  return NSGB_OK;
+}
+
+// Work of one tick, enqueued after the tick's tables are on the device.
+struct GradAction {
+  enum Kind { GACC_ZERO, FWD, ADJ, GREDUCE, FFT, FWD_DONE, ADJ_DONE } kind;
+  int member;          // GACC_ZERO, GREDUCE, FWD_DONE, ADJ_DONE
+  const nsgb_plan* plan;
+  int scheme;
+  size_t off;          // FWD, ADJ, FFT: table offset in the upload
+  int count;
+  AdjointArgs shape;   // ADJ: launch shape
+  const float* cur;    // FWD_DONE: the last step's u*
+};
+
+// Per-member view of its state (the layout of nsgb_rollout_grad).
+struct GradMemberCtx {
+  GradWs g;
+  StencilArgs a;
+  AdjointArgs b;
+  int nblk, adj_nblk;
+  size_t NN;
+};
+
+GradMemberCtx grad_member_ctx(const nsgb_grad_member& m) {
+  GradMemberCtx c;
+  c.g = carve_grad(m.plan, m.steps, m.every, m.state);
+  c.NN = (size_t)m.plan->N * m.plan->N;
+  c.a = stencil_args(m.plan, &m.phys);
+  c.a.theta = m.theta;
+  c.a.theta_len = m.theta_len;
+  c.nblk = stencil_nblocks(m.plan->N, c.a.tw, c.a.th);
+  c.b = AdjointArgs();
+  c.b.c = c.a.c;
+  c.b.scheme = c.a.scheme;
+  c.b.tw = m.plan->adj_w;
+  c.b.th = m.plan->adj_h;
+  c.b.theta = m.theta;
+  c.b.theta_len = m.theta_len;
+  c.b.gpart = c.g.gpart;
+  c.b.rhs = c.g.f.rhs;
+  c.adj_nblk = stencil_nblocks(m.plan->N, c.b.tw, c.b.th);
+  return c;
+}
+
+// Arguments of forward or recomputed step o (rollout_step's, with the
+// checkpoint or the stored state as u_out).
+StencilArgs grad_fwd_args(const nsgb_grad_member& m, const GradMemberCtx& c, const GradOp& o, bool& fft,
+                          const float*& out_us) {
+  const RolloutWs& w = c.g.f;
+  StencilArgs x = c.a;
+  const int s = o.s;
+  if (o.kind == GOP_FWD) {
+    x.us = s == 0 ? m.u0 : (((s - 1) % 2 == 0) ? w.usA : w.usB);
+    x.p = s == 0 ? nullptr : w.p;
+    x.us_out = (s % 2 == 0) ? w.usA : w.usB;
+    x.u_out = (s % m.every == 0) ? c.g.ckpt + (size_t)(s / m.every) * 2 * c.NN : nullptr;
+    fft = true;
+  } else {
+    const int r = s - o.s0;
+    x.us = r == 0 ? c.g.ckpt + (size_t)o.seg * 2 * c.NN : (((r - 1) % 2 == 0) ? w.usA : w.usB);
+    x.p = r == 0 ? nullptr : w.p;
+    x.us_out = (r % 2 == 0) ? w.usA : w.usB;
+    x.u_out = c.g.ustore + (size_t)r * 2 * c.NN;
+    fft = s + 1 < o.s1;
+  }
+  x.rhs = w.rhs;
+  x.jpart = w.jpart;
+  x.jpart_rows = w.steps;
+  x.step_ctr = nullptr;
+  x.step_fixed = s;
+  x.t_from_step = 1;
+  out_us = x.us_out;
+  return x;
+}
+
+// Arguments of adjoint step o (grad_enqueue's lambda ping-pong: the adjoint
+// step b = steps - 1 - s writes lamA for even b, lamB for odd b).
+AdjointArgs grad_adj_args(const nsgb_grad_member& m, const GradMemberCtx& c, const GradOp& o) {
+  AdjointArgs x = c.b;
+  const int s = o.s, b = m.steps - 1 - s;
+  x.lam = b == 0 ? nullptr : (((b - 1) % 2 == 0) ? c.g.lamA : c.g.lamB);
+  x.p = b >= 1 ? c.g.padj : nullptr;
+  x.u = (o.s1 - o.s0 == 1) ? c.g.ckpt + (size_t)o.seg * 2 * c.NN : c.g.ustore + (size_t)(s - o.s0) * 2 * c.NN;
+  x.lam_out = (s == 0 && m.dJdu0) ? m.dJdu0 : ((b % 2 == 0) ? c.g.lamA : c.g.lamB);
+  x.step = s;
+  x.gslot = b % kGradRows;
+  return x;
+}
+
+// Appends a device table (entries contiguous, sizeof(T) apart, as the
+// batched kernels index them) at a 16-byte aligned offset.
+template <class T>
+size_t put_table(std::vector<unsigned char>& buf, const std::vector<T>& v) {
+  const size_t off = (buf.size() + 15) & ~(size_t)15;
+  buf.resize(off + sizeof(T) * v.size());
+  std::memcpy(buf.data() + off, v.data(), sizeof(T) * v.size());
+  return off;
+}
+}  // namespace
+
+extern "C" {
+
+int nsgb_grad_ops(int steps, int every) {
+  if (steps < 1 || every < 1) return 0;
+  return grad_ops_total(steps, every);
+}
+
+size_t nsgb_grad_batch_workspace_bytes(int count, int ops) {
+  if (count < 1 || ops < 1) return 0;
+  return (size_t)ops * count * (2 * sizeof(SolveDev) + sizeof(AdjointArgs) + 5 * 16) + 256;
+}
+
+int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops, void* workspace,
+                            size_t ws_bytes, void* stream) {
+  if (int r = check_grad_members(members, count)) return r;
+  if (ops < 0) return fail(NSGB_ERR_INVALID_ARG, "ops must be >= 0");
+  if (ops == 0) return NSGB_OK;
+  if (int r = check_ws(workspace, ws_bytes, nsgb_grad_batch_workspace_bytes(count, ops))) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Each call uploads its argument tables from host memory.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  NSGB_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(NSGB_ERR_INVALID_ARG, "nsgb_grad_batch_advance does not run on a capturing stream");
+
+  std::vector<GradMemberCtx> ctx;
+  ctx.reserve(count);
+  std::vector<int> todo(count);
+  int maxtodo = 0;
+  for (int i = 0; i < count; ++i) {
+    ctx.push_back(grad_member_ctx(members[i]));
+    todo[i] = std::min(ops, grad_ops_total(members[i].steps, members[i].every) - members[i].done_ops);
+    maxtodo = std::max(maxtodo, todo[i]);
+  }
+  // Members grouped by plan (one launch shape and transform per group).
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return std::less<const nsgb_plan*>()(members[x].plan, members[y].plan); });
+
+  std::vector<unsigned char> buf;
+  buf.reserve(nsgb_grad_batch_workspace_bytes(count, std::min(ops, maxtodo)));
+  std::vector<GradAction> acts;
+  for (int k = 0; k < maxtodo; ++k) {
+    for (int g0 = 0; g0 < count;) {
+      const nsgb_plan* plan = members[order[g0]].plan;
+      int g1 = g0;
+      while (g1 < count && members[order[g1]].plan == plan) ++g1;
+      std::vector<SolveDev> fwd[2], fft;
+      std::vector<AdjointArgs> adj[2];
+      std::vector<GradAction> mid, post;
+      for (int q = g0; q < g1; ++q) {
+        const int i = order[q];
+        if (k >= todo[i]) continue;
+        const nsgb_grad_member& m = members[i];
+        const GradMemberCtx& c = ctx[i];
+        const GradOp o = grad_op(m.steps, m.every, m.done_ops + k);
+        const int sch = m.phys.scheme == NSGB_SCHEME_CENTRAL ? 0 : 1;
+        if (m.done_ops + k == m.steps) {
+          GradAction z{};
+          z.kind = GradAction::GACC_ZERO;
+          z.member = i;
+          acts.push_back(z);
+        }
+        if (o.kind != GOP_ADJ) {
+          bool do_fft = false;
+          const float* out_us = nullptr;
+          SolveDev d{};
+          d.st[0] = grad_fwd_args(m, c, o, do_fft, out_us);
+          fwd[sch].push_back(d);
+          if (do_fft) {
+            SolveDev f{};
+            f.fft = {c.g.f.rhs, (float2*)c.g.f.spec, c.g.f.p};
+            fft.push_back(f);
+          }
+          if (o.kind == GOP_FWD && o.s == m.steps - 1) {
+            GradAction z{};
+            z.kind = GradAction::FWD_DONE;
+            z.member = i;
+            z.cur = out_us;
+            post.push_back(z);
+          }
+        } else {
+          adj[sch].push_back(grad_adj_args(m, c, o));
+          const int b = m.steps - 1 - o.s;
+          if (b % kGradRows == kGradRows - 1) {
+            GradAction z{};
+            z.kind = GradAction::GREDUCE;
+            z.member = i;
+            mid.push_back(z);
+          }
+          if (o.s > 0) {
+            SolveDev f{};
+            f.fft = {c.g.f.rhs, (float2*)c.g.f.spec, c.g.padj};
+            fft.push_back(f);
+          } else {
+            GradAction z{};
+            z.kind = GradAction::ADJ_DONE;
+            z.member = i;
+            post.push_back(z);
+          }
+        }
+      }
+      for (int sch = 0; sch < 2; ++sch) {
+        if (fwd[sch].empty()) continue;
+        GradAction z{};
+        z.kind = GradAction::FWD;
+        z.plan = plan;
+        z.scheme = fwd[sch][0].st[0].scheme;
+        z.off = put_table(buf, fwd[sch]);
+        z.count = (int)fwd[sch].size();
+        acts.push_back(z);
+      }
+      for (int sch = 0; sch < 2; ++sch) {
+        if (adj[sch].empty()) continue;
+        GradAction z{};
+        z.kind = GradAction::ADJ;
+        z.plan = plan;
+        z.shape = adj[sch][0];
+        z.off = put_table(buf, adj[sch]);
+        z.count = (int)adj[sch].size();
+        acts.push_back(z);
+      }
+      acts.insert(acts.end(), mid.begin(), mid.end());
+      if (!fft.empty()) {
+        GradAction z{};
+        z.kind = GradAction::FFT;
+        z.plan = plan;
+        z.off = put_table(buf, fft);
+        z.count = (int)fft.size();
+        acts.push_back(z);
+      }
+      acts.insert(acts.end(), post.begin(), post.end());
+      g0 = g1;
+    }
+  }
+  if (buf.size() > ws_bytes) return fail(NSGB_ERR_WORKSPACE, "gradient batch tables exceed the workspace");
+  char* dev = (char*)workspace;
+  if (!buf.empty()) NSGB_CUDA(cudaMemcpyAsync(dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, st));
+  for (const GradAction& z : acts) {
+    switch (z.kind) {
+      case GradAction::GACC_ZERO:
+        NSGB_CUDA(cudaMemsetAsync(ctx[z.member].g.gacc, 0, 4 * sizeof(double), st));
+        break;
+      case GradAction::FWD:
+        NSGB_CUDA(launch_stencil_batch((const SolveDev*)(dev + z.off), z.count, 0, 0, z.scheme, z.plan->N,
+                                       z.plan->tile_w, z.plan->tile_h, st));
+        break;
+      case GradAction::ADJ:
+        NSGB_CUDA(launch_adjoint_batch(z.shape, (const AdjointArgs*)(dev + z.off), z.count, st));
+        break;
+      case GradAction::GREDUCE: {
+        const GradMemberCtx& c = ctx[z.member];
+        NSGB_CUDA(launch_greduce(c.g.gpart, c.adj_nblk, kGradRows, c.g.growsum, c.g.gacc, st));
+        break;
+      }
+      case GradAction::FFT:
+        NSGB_CUDA(poisson_fft_batch(z.plan->N, fft_launch(z.plan, nullptr, nullptr, nullptr),
+                                    (const SolveDev*)(dev + z.off), z.count, st));
+        break;
+      case GradAction::FWD_DONE: {
+        const nsgb_grad_member& m = members[z.member];
+        const GradMemberCtx& c = ctx[z.member];
+        if (m.u_final) NSGB_CUDA(launch_project(z.cur, c.g.f.p, m.u_final, c.a.c, st));
+        const double dx = m.plan->L / m.plan->N;
+        NSGB_CUDA(launch_jreduce(c.g.f.jpart, c.nblk, m.steps, c.g.f.jsteps, m.J, (double)m.phys.dt * dx * dx, st));
+        break;
+      }
+      case GradAction::ADJ_DONE: {
+        const nsgb_grad_member& m = members[z.member];
+        const GradMemberCtx& c = ctx[z.member];
+        NSGB_CUDA(launch_greduce(c.g.gpart, c.adj_nblk, m.steps % kGradRows, c.g.growsum, c.g.gacc, st));
+        NSGB_CUDA(launch_gfinal(c.g.gacc, m.theta_len, m.dJdtheta, st));
+        break;
+      }
+    }
+  }
+  return NSGB_OK;
+}
+
 // ----------------------------------------------------------- optimiser --
 namespace {
 struct OptWs {

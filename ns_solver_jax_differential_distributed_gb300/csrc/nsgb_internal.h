@@ -143,6 +143,11 @@ struct AdjointArgs {
   StepConsts c;
 };
 cudaError_t launch_adjoint_stencil(const AdjointArgs& a, cudaStream_t st);
+// The adjoint step of `count` solves in one launch (blockIdx.z = solve): tab
+// is a device table of their arguments; shape gives the launch shape, scheme
+// and N, which all entries share.  Each solve's results are those of its own
+// launch_adjoint_stencil.
+cudaError_t launch_adjoint_batch(const AdjointArgs& shape, const AdjointArgs* tab, int count, cudaStream_t st);
 // Adjoint shapes with tw >= NSGB_ROWS_MIN_W select the row-streaming adjoint
 // kernel: bands of min(tw, N) columns (a power of two <= NSGB_ADJ_ROWS_MAX_W;
 // its five input rings bound the band) by th rows.

@@ -175,3 +175,94 @@ def from_workload(members, scheme: str = None):
     unless `scheme` is given)."""
     return [SolveSpec(N=m.N, u0=m.u0(), theta=m.theta, nu=m.nu, dt=m.dt, scheme=scheme or m.scheme, L=m.L)
             for m in members]
+
+
+class GradientBatch:
+    """Gradient solves (forward with checkpoints + discrete adjoint, the
+    work of ``SingleCoreNSSolver.jit_gradient`` for a given u0) advanced
+    together by ``nsgb_grad_batch_advance``.  Solves may join at any call
+    (continuous batching); each solve's J and dJ/dtheta equal its own
+    ``nsgb_rollout_grad`` bit for bit.
+
+    ``add`` returns a solve id; ``advance(ops)`` moves every unfinished solve
+    by up to ``ops`` operations of its schedule (a forward, recomputed or
+    adjoint step each) and returns the ids that completed; ``result(id)``
+    gives (J, dJ/dtheta) as device tensors."""
+
+    def __init__(self, device=None):
+        self.device = torch.device(device or "cuda")
+        self._solves = {}
+        self._next = 0
+        self._ws = None
+
+    def add(self, u0, theta, steps: int, every: int, L: float, nu: float, dt: float, scheme,
+            mu0: float = 0.5, sigma0: float = 0.1, C: float = 1.0, want_du0: bool = False) -> int:
+        u0 = _native._cuda_f32(torch.as_tensor(u0, dtype=torch.float32).to(self.device), "u0")
+        theta = _native._cuda_f32(torch.as_tensor(theta, dtype=torch.float32).to(self.device), "theta")
+        N = _native._square(u0, "u0", 2)
+        plan = _native.get_plan(N, L, self.device)
+        steps, every = int(steps), int(every)
+        lib = _bind()
+        state = torch.empty(lib.nsgb_rollout_grad_workspace_bytes(plan.handle, steps, every),
+                            dtype=torch.uint8, device=self.device)
+        m = _native.GradMember()
+        m.plan = plan.handle.value
+        m.phys = _native.make_phys(L, nu, dt, scheme, mu0, sigma0, C)
+        rec = {
+            "u0": u0, "theta": theta, "plan": plan, "state": state,
+            "J": torch.empty((), dtype=torch.float32, device=self.device),
+            "g": torch.empty(theta.numel(), dtype=torch.float32, device=self.device),
+            "du0": torch.empty_like(u0) if want_du0 else None,
+            "total": int(lib.nsgb_grad_ops(steps, every)), "member": m,
+        }
+        m.u0 = u0.data_ptr()
+        m.theta = theta.data_ptr()
+        m.theta_len = theta.numel()
+        m.steps, m.every = steps, every
+        m.J = rec["J"].data_ptr()
+        m.u_final = None
+        m.dJdtheta = rec["g"].data_ptr()
+        m.dJdu0 = rec["du0"].data_ptr() if want_du0 else None
+        m.state = state.data_ptr()
+        m.done_ops = 0
+        sid = self._next
+        self._next += 1
+        self._solves[sid] = rec
+        return sid
+
+    def pending(self):
+        return [k for k, r in self._solves.items() if r["member"].done_ops < r["total"]]
+
+    def advance(self, ops: int):
+        ids = self.pending()
+        if not ids or ops <= 0:
+            return []
+        lib = _bind()
+        arr = (_native.GradMember * len(ids))(*[self._solves[k]["member"] for k in ids])
+        need = lib.nsgb_grad_batch_workspace_bytes(len(ids), int(ops))
+        if self._ws is None or self._ws.numel() < need:
+            self._ws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        _native.check("nsgb_grad_batch_advance", lib.nsgb_grad_batch_advance(
+            arr, len(ids), int(ops), self._ws.data_ptr(), self._ws.numel(), _native.stream_of(self.device)))
+        done = []
+        for k in ids:
+            r = self._solves[k]
+            r["member"].done_ops = min(r["total"], r["member"].done_ops + int(ops))
+            if r["member"].done_ops == r["total"]:
+                done.append(k)
+        return done
+
+    def run(self, ops_per_call: int = 64):
+        while self.pending():
+            self.advance(ops_per_call)
+
+    def result(self, sid: int):
+        r = self._solves[sid]
+        return r["J"], r["g"]
+
+    def du0(self, sid: int):
+        return self._solves[sid]["du0"]
+
+    def release(self, sid: int):
+        """Frees a finished (or abandoned) solve's device state."""
+        self._solves.pop(sid, None)

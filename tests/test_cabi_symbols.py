@@ -73,3 +73,21 @@ def test_misaligned_field_rejected_before_launch(lib):
     rc = L.nsgb_rollout(ctypes.addressof(dummy_plan), ctypes.byref(ph), 0x1004, ctypes.addressof(theta), 2, 1,
                         0x2000, 0x3000, 0x4000, 1 << 20, 0, None)
     assert rc == 1 and b"16-byte aligned" in L.nsgb_last_error()
+
+
+def _grad_ops(steps, every):
+    """Operations of a gradient solve: forward steps, then per checkpoint
+    segment its recomputed steps (none for one step) and adjoint steps."""
+    segs = [min(every, steps - s0) for s0 in range(0, steps, every)]
+    return steps + sum(1 if n == 1 else 2 * n for n in segs)
+
+
+def test_grad_batch_schedule_and_arguments(lib):
+    L = _native.lib()
+    for steps, every in [(1, 1), (5, 1), (10, 4), (12, 4), (7, 50), (1000, 50), (999, 7)]:
+        assert L.nsgb_grad_ops(steps, every) == _grad_ops(steps, every)
+    assert L.nsgb_grad_ops(0, 1) == 0 and L.nsgb_grad_ops(4, 0) == 0
+    assert L.nsgb_grad_batch_workspace_bytes(0, 8) == 0
+    assert L.nsgb_grad_batch_workspace_bytes(3, 8) > 0
+    assert L.nsgb_grad_batch_advance(None, 1, 4, None, 0, None) == 1
+    assert b"empty" in L.nsgb_last_error()
