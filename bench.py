@@ -60,6 +60,8 @@ def parse_args(argv=None):
                          "reference's optimiser study on the device")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals")
+    ap.add_argument("--grad-mode", choices=["batched", "workers"], default="batched",
+                    help="serve: gradient requests batched in lock-step, or one per worker thread")
     return ap.parse_args(argv)
 
 
@@ -632,9 +634,9 @@ def run_serve(args):
     _build.build()
     dev = torch.device("cuda", 0)
     for N in (128, 256, 512, 1024, 2048):
-        autotune.tune(N, 2 * math.pi, "central", dev)
+        autotune.tune(N, 2 * math.pi, "upwind", dev)
     reqs = serve.make_trace(rate=args.rate, duration=args.duration, seed=7)
-    srv = serve.Server(dev, hbm_budget=150e9)
+    srv = serve.Server(dev, hbm_budget=150e9, grad_mode=args.grad_mode)
     for N in (128, 256, 512, 1024, 2048):
         for s in range(16):
             srv.u0.get(N, s)
@@ -658,7 +660,9 @@ def run_serve(args):
                  "clocks": clock_info,
                  "config": {"workload": "serving", "arrivals": f"Poisson {args.rate} req/s for {args.duration} s",
                             "N": "uniform over {128,256,512,1024,2048}", "steps": "U[100,2000]",
-                            "grad_fraction": 0.3, "hbm_budget_bytes": 150e9, "dt": 1e-3}})
+                            "grad_fraction": 0.3, "hbm_budget_bytes": 150e9, "scheme": "upwind",
+                            "dt": "stable step of each request's N and nu (cfl 0.4, v_max 4)",
+                            "grad_mode": args.grad_mode, "grad_checkpoint_every": serve.GRAD_EVERY}})
     return summ
 
 

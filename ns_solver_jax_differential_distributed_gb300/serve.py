@@ -10,9 +10,13 @@ time.  A scheduler thread owns the GPU:
   active forward request by up to ``slice_steps`` steps in one
   ``nsgb_ensemble_advance`` call (one batched launch per stage per group of
   equal N), so requests that arrive while others run join at the next tick;
-* gradient requests run ``nsgb_rollout_grad`` (forward with checkpoints +
-  discrete adjoint) on worker threads, each with its own CUDA stream, so
-  their kernels overlap the batched forward work on the device;
+* gradient requests (forward with checkpoints + discrete adjoint) are
+  continuously batched the same way on a second CUDA stream: each tick moves
+  every active gradient request by up to ``grad_slice_ops`` operations of its
+  schedule in one ``nsgb_grad_batch_advance`` call (one batched launch per
+  kernel per group of equal N), overlapping the forward tick on the device;
+  ``grad_mode="workers"`` instead runs each one as ``nsgb_rollout_grad`` on
+  worker threads with their own streams;
 * completion is detected with CUDA events; memory returns to the budget.
 
 Failures are isolated per request: every request ends with a ``status`` --
@@ -134,9 +138,16 @@ class _U0Cache:
             return self._c[key]
 
 
+GRAD_EVERY = 50  # checkpoint interval of served gradient requests
+
+
 class Server:
     def __init__(self, device=None, hbm_budget: float = 150e9, slice_steps: int = 32,
-                 max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 8):
+                 max_active_cells: float = 96 * 2 ** 20, grad_workers: int = 8,
+                 grad_mode: str = "batched", grad_slice_ops: int = 32,
+                 max_active_grad_cells: float = 48 * 2 ** 20):
+        if grad_mode not in ("batched", "workers"):
+            raise ValueError(f"grad_mode must be 'batched' or 'workers', got {grad_mode!r}")
         dev = torch.device(device or "cuda")
         if dev.index is None:
             dev = torch.device("cuda", torch.cuda.current_device())
@@ -145,6 +156,9 @@ class Server:
         self.slice = int(slice_steps)
         self.max_active_cells = float(max_active_cells)
         self.grad_workers = int(grad_workers)
+        self.grad_mode = grad_mode
+        self.grad_slice = int(grad_slice_ops)
+        self.max_active_grad_cells = float(max_active_grad_cells)
         self.u0 = _U0Cache(self.device)
         self.used = 0.0
         self.peak_used = 0.0
@@ -153,9 +167,10 @@ class Server:
         self._cancel = set()
 
     def cancel(self, rid: int) -> None:
-        """Cancel request `rid`: dropped if still queued or advancing as a
-        forward solve (its memory returns to the budget at the next tick); a
-        gradient already running completes and is then reported cancelled."""
+        """Cancel request `rid`: dropped if still queued or advancing in a
+        batch (its memory returns to the budget at the next tick); a gradient
+        already running on a worker thread (grad_mode="workers") completes and
+        is then reported cancelled."""
         with self._lock:
             self._cancel.add(int(rid))
 
@@ -179,7 +194,7 @@ class Server:
 
     def _grad_bytes(self, r: Request) -> int:
         plan = _native.get_plan(r.N, r.L, self.device)
-        return int(_native.lib().nsgb_rollout_grad_workspace_bytes(plan.handle, r.steps, 50) + 4096)
+        return int(_native.lib().nsgb_rollout_grad_workspace_bytes(plan.handle, r.steps, GRAD_EVERY) + 4096)
 
     # -- gradient workers
     def _grad_worker(self, q: "queue.Queue", done_q: "queue.Queue"):
@@ -194,7 +209,7 @@ class Server:
                 with torch.cuda.stream(stream):
                     u0 = self._initial(r)
                     th = torch.from_numpy(r.theta).to(self.device, non_blocking=True)
-                    J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, 50, r.L, r.nu, r.dt, r.scheme,
+                    J, g, _, _ = _native.rollout_grad_raw(u0, th, r.steps, GRAD_EVERY, r.L, r.nu, r.dt, r.scheme,
                                                           want_u_final=False, own_workspace=True)
                     Jh, gh = J.to("cpu", non_blocking=True), g.to("cpu", non_blocking=True)
                     ev = torch.cuda.Event()
@@ -205,6 +220,31 @@ class Server:
             except Exception as exc:  # this request fails; the worker serves on
                 done_q.put((r, nbytes, exc))
 
+    def _admit_grad(self, r: Request, gstream) -> dict:
+        """Device state of a batched gradient request, allocated on the
+        gradient stream (raises if an allocation fails)."""
+        L = _native.lib()
+        with torch.cuda.stream(gstream):
+            plan = _native.get_plan(r.N, r.L, self.device)
+            st_bytes = L.nsgb_rollout_grad_workspace_bytes(plan.handle, r.steps, GRAD_EVERY)
+            state = self._alloc(r, (st_bytes,), torch.uint8)
+            th = torch.from_numpy(np.asarray(r.theta, dtype=np.float32)).to(self.device)
+            J = self._alloc(r, (), torch.float32)
+            g = self._alloc(r, (th.numel(),), torch.float32)
+            u0 = self._initial(r)
+        m = _native.GradMember()
+        m.plan = plan.handle.value
+        m.phys = _native.make_phys(r.L, r.nu, r.dt, r.scheme)
+        m.u0 = u0.data_ptr()
+        m.theta = th.data_ptr()
+        m.theta_len = th.numel()
+        m.steps, m.every = r.steps, GRAD_EVERY
+        m.J, m.u_final, m.dJdtheta, m.dJdu0 = J.data_ptr(), None, g.data_ptr(), None
+        m.state = state.data_ptr()
+        m.done_ops = 0
+        return dict(r=r, m=m, state=state, th=th, J=J, g=g, u0=u0, plan=plan,
+                    total=int(L.nsgb_grad_ops(r.steps, GRAD_EVERY)))
+
     def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None):
         """Serve `requests` (sorted by arrival).  With realtime, arrivals
         follow the wall clock; otherwise all are available at once.  Stops
@@ -214,8 +254,15 @@ class Server:
         nxt = 0
         active = []          # forward requests: dict(r, state, done, out, J)
         grad_q, grad_done = queue.Queue(), queue.Queue()
-        workers = [threading.Thread(target=self._grad_worker, args=(grad_q, grad_done), daemon=True)
-                   for _ in range(self.grad_workers)]
+        batched = self.grad_mode == "batched"
+        workers = [] if batched else [
+            threading.Thread(target=self._grad_worker, args=(grad_q, grad_done), daemon=True)
+            for _ in range(self.grad_workers)]
+        gstream = torch.cuda.Stream(self.device) if batched else None
+        gactive = []         # batched gradient requests: dict(r, m, state, ...)
+        gfinishing = []      # (event, entry, J on host, dJ/dtheta on host)
+        gws = None
+        gticks = collections.deque()
         for w in workers:
             w.start()
         grads_inflight = 0
@@ -235,6 +282,7 @@ class Server:
                 nxt += 1
             # admission (FIFO): memory budget, and a cap on active forward work
             act_cells = sum(a["r"].N ** 2 for a in active)
+            grad_cells = sum(a["r"].N ** 2 for a in gactive)
             while pending and self._cancelled(pending[0]):
                 r = pending.popleft()
                 r.status, r.t_done = "cancelled", time.perf_counter() - t0
@@ -248,11 +296,28 @@ class Server:
                     break
                 if r.kind == "forward" and act_cells + r.N ** 2 > self.max_active_cells and active:
                     break
-                if r.kind == "grad" and grads_inflight >= 2 * self.grad_workers:
+                if r.kind == "grad" and not batched and grads_inflight >= 2 * self.grad_workers:
+                    break
+                if (r.kind == "grad" and batched and gactive
+                        and grad_cells + r.N ** 2 > self.max_active_grad_cells):
                     break
                 pending.popleft()
                 r.t_admit = time.perf_counter() - t0
-                if r.kind == "grad":
+                if r.kind == "grad" and batched:
+                    try:
+                        entry = self._admit_grad(r, gstream)
+                    except Exception as exc:  # this request fails; nothing was charged
+                        r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
+                        r.t_done = time.perf_counter() - t0
+                        completed.append(r)
+                        self.stats["failed"] += 1
+                        continue
+                    entry["nb"] = nb
+                    self.used += nb
+                    grads_inflight += 1
+                    gactive.append(entry)
+                    grad_cells += r.N ** 2
+                elif r.kind == "grad":
                     self.used += nb
                     grads_inflight += 1
                     grad_q.put((r, nb))
@@ -274,7 +339,18 @@ class Server:
                     active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=0, nb=nb, plan=plan))
                     act_cells += r.N ** 2
                 self.peak_used = max(self.peak_used, self.used)
-            # cancelled forward requests leave before the next tick
+            # cancelled requests leave before the next tick
+            if gactive:
+                keep = []
+                for a in gactive:
+                    if self._cancelled(a["r"]):
+                        a["r"].status, a["r"].t_done = "cancelled", time.perf_counter() - t0
+                        self.used -= a["nb"]
+                        grads_inflight -= 1
+                        completed.append(a["r"])
+                    else:
+                        keep.append(a)
+                gactive = keep
             if active:
                 keep = []
                 for a in active:
@@ -309,6 +385,7 @@ class Server:
                 for a in active:
                     a["done"] = min(a["r"].steps, a["done"] + self.slice)
                     if a["done"] >= a["r"].steps:
+                        a["J_host"] = a["J"].to("cpu", non_blocking=True)
                         ev = torch.cuda.Event()
                         ev.record(stream)
                         finishing.append((ev, a))
@@ -323,12 +400,39 @@ class Server:
                 ticks.append(tev)
                 if len(ticks) > 2:
                     ticks.popleft().synchronize()
+            # one tick of continuous batching over the active gradient requests
+            if gactive:
+                arr = (_native.GradMember * len(gactive))(*[a["m"] for a in gactive])
+                need = L.nsgb_grad_batch_workspace_bytes(len(gactive), self.grad_slice)
+                with torch.cuda.stream(gstream):
+                    if gws is None or gws.numel() < need:
+                        gws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
+                    _native.check("nsgb_grad_batch_advance", L.nsgb_grad_batch_advance(
+                        arr, len(gactive), self.grad_slice, gws.data_ptr(), gws.numel(), gstream.cuda_stream))
+                    keep = []
+                    for a in gactive:
+                        a["m"].done_ops = min(a["total"], a["m"].done_ops + self.grad_slice)
+                        if a["m"].done_ops >= a["total"]:
+                            Jh = a["J"].to("cpu", non_blocking=True)
+                            gh = a["g"].to("cpu", non_blocking=True)
+                            ev = torch.cuda.Event()
+                            ev.record(gstream)
+                            gfinishing.append((ev, a, Jh, gh))
+                        else:
+                            keep.append(a)
+                    gactive = keep
+                    self.stats["grad_ticks"] += 1
+                    tev = torch.cuda.Event()
+                    tev.record(gstream)
+                    gticks.append(tev)
+                if len(gticks) > 2:
+                    gticks.popleft().synchronize()
             # completions
             still = []
             for ev, a in finishing:
                 if ev.query():
                     r = a["r"]
-                    r.J = float(a["J"])
+                    r.J = float(a["J_host"])
                     r.u_final = a["out"]
                     r.status = "ok" if math.isfinite(r.J) else "nonfinite"
                     r.t_done = time.perf_counter() - t0
@@ -337,6 +441,23 @@ class Server:
                 else:
                     still.append((ev, a))
             finishing = still
+            still = []
+            for ev, a, Jh, gh in gfinishing:
+                if ev.query():
+                    r = a["r"]
+                    r.J, r.grad = float(Jh), gh.numpy().copy()
+                    if self._cancelled(r):
+                        r.status = "cancelled"
+                    else:
+                        ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
+                        r.status = "ok" if ok else "nonfinite"
+                    r.t_done = time.perf_counter() - t0
+                    self.used -= a["nb"]
+                    grads_inflight -= 1
+                    completed.append(r)
+                else:
+                    still.append((ev, a, Jh, gh))
+            gfinishing = still
             while not grad_done.empty():
                 r, nb, exc = grad_done.get()
                 if exc is not None:
@@ -357,7 +478,7 @@ class Server:
                 break
             if drain_limit is not None and now > last_arrival + drain_limit:
                 break
-            if not active and not finishing:
+            if not active and not finishing and not gactive and not gfinishing:
                 time.sleep(0.0005)
         for _ in workers:
             grad_q.put(None)

@@ -68,7 +68,7 @@ def test_failures_are_isolated(serve):
     reqs = _trace(serve, 30)
     fwd = [r for r in reqs if r.kind == "forward"]
     grd = [r for r in reqs if r.kind == "grad"]
-    nan_f, nan_g, boom, gone = fwd[1], grd[0], fwd[3], fwd[5]
+    nan_f, nan_g, boom, boom_g, gone = fwd[1], grd[0], fwd[3], grd[1], fwd[5]
     srv = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128, grad_workers=2)
     for r in (nan_f, nan_g):
         u0 = srv.u0.get(r.N, r.seed).clone()
@@ -77,7 +77,7 @@ def test_failures_are_isolated(serve):
     real_alloc = srv._alloc
 
     def alloc(r, shape, dtype):
-        if r.rid == boom.rid:
+        if r.rid in (boom.rid, boom_g.rid):
             raise torch.cuda.OutOfMemoryError("injected allocation failure")
         return real_alloc(r, shape, dtype)
 
@@ -87,11 +87,12 @@ def test_failures_are_isolated(serve):
     assert len(done) == len(reqs)
     by = {r.rid: r for r in done}
     assert by[nan_f.rid].status == "nonfinite" and by[nan_g.rid].status == "nonfinite"
-    assert by[boom.rid].status == "failed" and "injected" in by[boom.rid].error
+    for x in (boom, boom_g):
+        assert by[x.rid].status == "failed" and "injected" in by[x.rid].error
     assert by[gone.rid].status == "cancelled"
     assert srv.used == pytest.approx(0.0)
     for rid, r in by.items():
-        if rid in (nan_f.rid, nan_g.rid, boom.rid, gone.rid):
+        if rid in (nan_f.rid, nan_g.rid, boom.rid, boom_g.rid, gone.rid):
             continue
         assert r.status == "ok" and r.J == ref[rid].J, rid
         if r.kind == "grad":
@@ -99,7 +100,27 @@ def test_failures_are_isolated(serve):
         else:
             assert torch.equal(r.u_final, ref[rid].u_final), rid
     s = serve.summarize(reqs, done, 1.0)
-    assert s["statuses"] == {"ok": len(reqs) - 4, "nonfinite": 2, "failed": 1, "cancelled": 1}
+    assert s["statuses"] == {"ok": len(reqs) - 5, "nonfinite": 2, "failed": 2, "cancelled": 1}
+
+
+def test_batched_and_worker_gradients_agree(serve):
+    """Gradient requests served by the batched path (several in flight at
+    once, work split into uneven slices) and by worker threads running
+    nsgb_rollout_grad give the same bits."""
+    kw = dict(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128)
+    a = serve.Server(grad_mode="batched", grad_slice_ops=5, **kw)
+    da, trace = a.run(_trace(serve, 30), realtime=False)
+    b = serve.Server(grad_mode="workers", grad_workers=2, **kw)
+    db, _ = b.run(_trace(serve, 30), realtime=False)
+    assert max(t[3] for t in trace) > 1, "gradient requests were never batched together"
+    ga = {r.rid: r for r in da if r.kind == "grad"}
+    gb = {r.rid: r for r in db if r.kind == "grad"}
+    assert len(ga) >= 5 and ga.keys() == gb.keys()
+    for rid in ga:
+        assert ga[rid].status == gb[rid].status == "ok"
+        assert ga[rid].J == gb[rid].J and np.array_equal(ga[rid].grad, gb[rid].grad), rid
+    with pytest.raises(ValueError):
+        serve.Server(grad_mode="threads")
 
 
 def test_summary(serve):
