@@ -460,6 +460,7 @@ def run_grad(args):
     torch.cuda.reset_peak_memory_stats(dev)
     t_all, (_, g_all) = timed(lambda: solver_all.gradient(u0, th))
     mem_all = torch.cuda.max_memory_allocated(dev)
+    batch = grad_batch_compare(dev, reps)
     clock_info = clocks.stop()
     g = g.double().cpu().numpy()
     ref = None
@@ -482,7 +483,66 @@ def run_grad(args):
             "auto_checkpoint": {"checkpoint_every": every_auto, "gradient_ms": t_all,
                                 "ratio_to_forward": t_all / t_fwd, "peak_mem_gradient_bytes": mem_all,
                                 "max_abs_diff_vs_every_50": float(np.abs(g_all.double().cpu().numpy() - g).max())},
+            "batched_gradients": batch,
             "clocks": clock_info, "dtype": "f32", "data": "synthetic"}
+
+
+def grad_batch_compare(dev, reps: int, count: int = 16, seed: int = 5) -> dict:
+    """`count` gradient requests drawn like the serving trace's small and
+    mid sizes (N uniform over {128, 256, 512}, steps U[100, 400], upwind,
+    the stable time step, checkpoints every 50): solved one after another by
+    nsgb_rollout_grad, and together by nsgb_grad_batch_advance (lock-step,
+    one batched launch per kernel per size group).  Both are timed with CUDA
+    events on the device (host gaps included); results must agree bit for
+    bit."""
+    import torch
+    from ns_solver_jax_differential_distributed_gb300 import _native, autotune, ensemble, serve
+    from ns_solver_jax_differential_distributed_gb300.workloads import spectral_u0, theta_draw
+    L = 2 * math.pi
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        N = int(rng.choice([128, 256, 512]))
+        steps = int(rng.integers(100, 401))
+        th = theta_draw(1e-3, seed=i)
+        nu = float(th[2])
+        reqs.append(dict(N=N, steps=steps, nu=nu, dt=serve.stable_dt(N, L, nu),
+                         u0=torch.from_numpy(spectral_u0(N, min(32, N // 4), i)).to(dev),
+                         th=torch.from_numpy(th).to(dev)))
+    for N in sorted({r["N"] for r in reqs}):
+        autotune.tune(N, L, "upwind", dev)
+
+    def sequential():
+        return [_native.rollout_grad_raw(r["u0"], r["th"], r["steps"], 50, L, r["nu"], r["dt"], "upwind",
+                                         want_u_final=False)[:2] for r in reqs]
+
+    def batched():
+        gb = ensemble.GradientBatch(dev)
+        ids = [gb.add(r["u0"], r["th"], r["steps"], 50, L, r["nu"], r["dt"], "upwind") for r in reqs]
+        gb.run(64)
+        return [gb.result(k) for k in ids]
+
+    def timed(fn):
+        for _ in range(3):
+            out = fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            out = [(J.clone(), g.clone()) for J, g in fn()]
+        e1.record()
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / reps, out
+
+    t_seq, out_seq = timed(sequential)
+    t_bat, out_bat = timed(batched)
+    same = all(torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) for a, b in zip(out_seq, out_bat))
+    sizes = {}
+    for r in reqs:
+        sizes[str(r["N"])] = sizes.get(str(r["N"]), 0) + 1
+    return {"requests": count, "sizes": sizes, "steps": "U[100,400]", "checkpoint_every": 50,
+            "sequential_ms": t_seq, "batched_ms": t_bat, "speedup": t_seq / t_bat,
+            "results_bitwise_equal": bool(same), "reps": reps}
 
 
 def run_optimize(args):
