@@ -42,6 +42,7 @@ extern "C" {
 #define NSGB_ERR_OOM 4
 #define NSGB_ERR_WORKSPACE 5
 #define NSGB_ERR_NONFINITE 6
+#define NSGB_ERR_BOUNDS 7    /* bounds-checking build: a kernel accessed memory outside the valid ranges */
 
 #define NSGB_MAX_N 8192 /* largest grid a plan accepts */
 
@@ -199,6 +200,21 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
                       const float* theta, int theta_len, int steps, int every, int phases,
                       float* J, float* u_final, float* dJdtheta, float* dJdu0, void* workspace,
                       size_t workspace_bytes, void* stream);
+
+/* Bounds checking (no counterpart in the reference).  The library built with
+ * NSGB_CHECK_BOUNDS (libnsgb_checked.so) checks every global-memory access of
+ * its kernels against the device ranges it knows to be valid: its plans'
+ * tables, its static scratch, and the ranges registered here.  An access
+ * outside all of them is skipped (a load yields zero) and counted, and the
+ * entry point that launched it waits for its stream and returns
+ * NSGB_ERR_BOUNDS with the first bad address, its size and the source line of
+ * the access, instead of faulting.  In the normal build these calls do
+ * nothing and return NSGB_OK; nsgb_bounds_checking() tells the builds apart
+ * (1 when checking).  Registered ranges are [base, base + bytes). */
+int nsgb_bounds_checking(void);
+int nsgb_bounds_register(const void* base, size_t bytes);
+int nsgb_bounds_unregister(const void* base);
+int nsgb_bounds_clear(void);
 
 /* One gradient solve of a batch advanced by nsgb_grad_batch_advance. */
 typedef struct nsgb_grad_member {

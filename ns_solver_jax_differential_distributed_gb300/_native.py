@@ -106,6 +106,10 @@ SIGNATURES = {
     "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_poisson_noalloc": ([_I, _D, _P, _P, _P], _I),
+    "nsgb_bounds_checking": ([], _I),
+    "nsgb_bounds_register": ([_P, _S], _I),
+    "nsgb_bounds_unregister": ([_P], _I),
+    "nsgb_bounds_clear": ([], _I),
     "nsgb_grad_ops": ([_I, _I], _I),
     "nsgb_grad_batch_workspace_bytes": ([_I, _I], _S),
     "nsgb_grad_batch_advance": ([ctypes.POINTER(GradMember), _I, _I, _P, _S, _P], _I),

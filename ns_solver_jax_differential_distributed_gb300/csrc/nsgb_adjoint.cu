@@ -136,11 +136,11 @@ __device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
 
   const float dt = c.dt;
   const float jscale = c.jscale;  // float32(dt * dx^2) = dJ/du_x / f_x
-  const float nu = (a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float nu = (a.theta_len == 3) ? gldg(a.theta + 2) : c.nu;
   const float cL = fmul(c.dtdx2, nu);                              // dt nu / dx^2
   const float cA = SCHEME == NSGB_SCHEME_CENTRAL ? c.cAc : c.cAu;  // dt / h
   const float t = fmul((float)a.step, dt);
-  const float A = __ldg(a.theta), B = __ldg(a.theta + 1);
+  const float A = gldg(a.theta), B = gldg(a.theta + 1);
 
   const bool has_lam = a.lam != nullptr;
   const bool has_p = a.p != nullptr;
@@ -148,8 +148,7 @@ __device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
   if (has_p) {
     const float* __restrict__ pp = a.p;
     forflat<PH, G>(tid, [&](int r, int q) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(
-          pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M)));
+      const float4 v = gldg4(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M));
       *reinterpret_cast<float4*>(sP + r * W4 + 4 * q) = v;
     });
   }
@@ -159,11 +158,11 @@ __device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
     forflat<UH, G>(tid, [&](int r, int q) {
       const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 4 + 4 * q) & M);
       const int o = r * W4 + 4 * q;
-      *reinterpret_cast<float4*>(sUx + o) = __ldg(reinterpret_cast<const float4*>(u + g));
-      *reinterpret_cast<float4*>(sUy + o) = __ldg(reinterpret_cast<const float4*>(u + NN + g));
+      *reinterpret_cast<float4*>(sUx + o) = gldg4(u + g);
+      *reinterpret_cast<float4*>(sUy + o) = gldg4(u + NN + g);
       const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-      *reinterpret_cast<float4*>(sMx + o) = has_lam ? __ldg(reinterpret_cast<const float4*>(lam + g)) : z;
-      *reinterpret_cast<float4*>(sMy + o) = has_lam ? __ldg(reinterpret_cast<const float4*>(lam + NN + g)) : z;
+      *reinterpret_cast<float4*>(sMx + o) = has_lam ? gldg4(lam + g) : z;
+      *reinterpret_cast<float4*>(sMy + o) = has_lam ? gldg4(lam + NN + g) : z;
     });
   }
   {
@@ -225,9 +224,9 @@ __device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
     forflat<TH, TW>(tid, [&](int r, int cc) {
       const int o = (r + 1) * SW + (cc + 1);
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      lo[g] = sLx[o];
-      lo[NN + g] = sLy[o];
-      rhs[g] = fused_rhs(sLx[o + SW], sLx[o - SW], sLy[o + 1], sLy[o - 1], c.cD);
+      gst(lo + g, sLx[o]);
+      gst(lo + NN + g, sLy[o]);
+      gst(rhs + g, fused_rhs(sLx[o + SW], sLx[o - SW], sLy[o + 1], sLy[o - 1], c.cD));
     });
   }
 
@@ -248,10 +247,10 @@ __device__ __forceinline__ void adjoint_body(const AdjointArgs& a) {
     if (tx == 0) {
       const int nblk = gridDim.x * gridDim.y;
       double* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
-      gp[0] = (double)v0.hi + (double)v0.lo;
-      gp[1] = (double)v1.hi + (double)v1.lo;
+      gst(gp, (double)v0.hi + (double)v0.lo);
+      gst(gp + 1, (double)v1.hi + (double)v1.lo);
       // the nu partial carries the Laplacian's 1/dx^2 and the step's dt
-      gp[2] = ((double)v2.hi + (double)v2.lo) * ((double)dt * (double)c.rdx2);
+      gst(gp + 2, ((double)v2.hi + (double)v2.lo) * ((double)dt * (double)c.rdx2));
     }
   }
 }
@@ -362,11 +361,11 @@ __device__ __forceinline__ void adjoint_rows_body(const AdjointArgs& a) {
 
   const float dt = c.dt;
   const float jscale = c.jscale;
-  const float nu = (a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float nu = (a.theta_len == 3) ? gldg(a.theta + 2) : c.nu;
   const float cL = fmul(c.dtdx2, nu);
   const float cA = SCHEME == NSGB_SCHEME_CENTRAL ? c.cAc : c.cAu;
   const float tf = fmul((float)a.step, dt);
-  const float A = __ldg(a.theta), B = __ldg(a.theta + 1);
+  const float A = gldg(a.theta), B = gldg(a.theta + 1);
   {
     const ForcingRow fr = forcing_time(A, B, tf, c);
     for (int k = tid; k < r1 - r0 + 2; k += blockDim.x) sF[k] = forcing_fx((r0 - 1 + k) & M, fr, c);
@@ -534,9 +533,9 @@ __device__ __forceinline__ void adjoint_rows_body(const AdjointArgs& a) {
     if (lane == 0) {
       const int nblk = gridDim.x * gridDim.y;
       double* gp = a.gpart + ((size_t)a.gslot * nblk + blockIdx.y * gridDim.x + blockIdx.x) * 3;
-      gp[0] = (double)v0.hi + (double)v0.lo;
-      gp[1] = (double)v1.hi + (double)v1.lo;
-      gp[2] = ((double)v2.hi + (double)v2.lo) * ((double)dt * (double)c.rdx2);
+      gst(gp, (double)v0.hi + (double)v0.lo);
+      gst(gp + 1, (double)v1.hi + (double)v1.lo);
+      gst(gp + 2, ((double)v2.hi + (double)v2.lo) * ((double)dt * (double)c.rdx2));
     }
   }
 }
@@ -597,9 +596,9 @@ __global__ void k_greduce_rows(const double* __restrict__ gpart, int nblk, doubl
   const double* base = gpart + (size_t)blockIdx.x * nblk * 3;
   double v0 = 0, v1 = 0, v2 = 0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-    v0 += base[3 * b];
-    v1 += base[3 * b + 1];
-    v2 += base[3 * b + 2];
+    v0 += gld(base + 3 * b);
+    v1 += gld(base + 3 * b + 1);
+    v2 += gld(base + 3 * b + 2);
   }
   red[0][threadIdx.x] = v0;
   red[1][threadIdx.x] = v1;
@@ -613,14 +612,14 @@ __global__ void k_greduce_rows(const double* __restrict__ gpart, int nblk, doubl
     }
     __syncthreads();
   }
-  if (threadIdx.x < 3) rowsum[3 * blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x < 3) gst(rowsum + 3 * blockIdx.x + threadIdx.x, red[threadIdx.x][0]);
 }
 
 __global__ void k_greduce_acc(const double* __restrict__ rowsum, int nrows, double* __restrict__ gacc) {
   if (threadIdx.x >= 3) return;
-  double g = gacc[threadIdx.x];
-  for (int row = 0; row < nrows; ++row) g += rowsum[3 * row + threadIdx.x];
-  gacc[threadIdx.x] = g;
+  double g = gld(gacc + threadIdx.x);
+  for (int row = 0; row < nrows; ++row) g += gld(rowsum + 3 * row + threadIdx.x);
+  gst(gacc + threadIdx.x, g);
 }
 
 cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* rowsum, double* gacc,
@@ -632,12 +631,14 @@ cudaError_t launch_greduce(const double* gpart, int nblk, int nrows, double* row
 }
 
 __global__ void k_gfinal(const double* __restrict__ gacc, int theta_len, float* __restrict__ dJ) {
-  for (int k = 0; k < theta_len; ++k) dJ[k] = (float)gacc[k];
+  for (int k = 0; k < theta_len; ++k) gst(dJ + k, (float)gld(gacc + k));
 }
 
 cudaError_t launch_gfinal(const double* gacc, int theta_len, float* dJ, cudaStream_t st) {
   k_gfinal<<<1, 1, 0, st>>>(gacc, theta_len, dJ);
   return cudaGetLastError();
 }
+
+NSGB_BOUNDS_UNIT(adjoint, 3)
 
 }  // namespace nsgb

@@ -582,6 +582,113 @@ cudaError_t fused_step(const nsgb_plan* plan, const StencilArgs& a, const float*
 
 void nsgb::set_last_error(const char* msg) { g_last_error = msg; }
 
+// ------------------------------------------------------ bounds checking --
+// The bounds-checking build keeps the valid device ranges -- the library's
+// own (plan tables, the no-allocation scratch) and the caller's
+// (nsgb_bounds_register) -- and uploads them to every translation unit's
+// table whenever they change, after the device has finished the work that
+// reads the old table.  Every entry point that enqueues work ends with
+// finish_call: it waits for its stream and turns recorded out-of-range
+// accesses into NSGB_ERR_BOUNDS.
+#ifdef NSGB_CHECK_BOUNDS
+namespace nsgb {
+cudaError_t bounds_upload_stencil(const bounds::Table& t);
+cudaError_t bounds_upload_fft(const bounds::Table& t);
+cudaError_t bounds_upload_adjoint(const bounds::Table& t);
+cudaError_t bounds_upload_fused(const bounds::Table& t);
+cudaError_t bounds_upload_optim(const bounds::Table& t);
+}  // namespace nsgb
+namespace {
+std::mutex g_bounds_mu;
+std::vector<std::pair<unsigned long long, unsigned long long>> g_bounds_lib, g_bounds_caller;
+unsigned long long* g_bounds_report = nullptr;
+
+int bounds_upload_locked() {
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) return cuda_fail(e, "bounds table update");
+  if (!g_bounds_report) {
+    if ((e = cudaMalloc(&g_bounds_report, 4 * sizeof(unsigned long long))) != cudaSuccess)
+      return cuda_fail(e, "bounds report");
+    if ((e = cudaMemset(g_bounds_report, 0, 4 * sizeof(unsigned long long))) != cudaSuccess)
+      return cuda_fail(e, "bounds report");
+  }
+  bounds::Table t{};
+  for (const auto* v : {&g_bounds_lib, &g_bounds_caller})
+    for (const auto& r : *v) {
+      if (t.n == bounds::kMaxRanges) return fail(NSGB_ERR_INVALID_ARG, "more than %d checked ranges", bounds::kMaxRanges);
+      t.lo[t.n] = r.first;
+      t.hi[t.n] = r.second;
+      ++t.n;
+    }
+  t.report = g_bounds_report;
+  for (auto up : {bounds_upload_stencil, bounds_upload_fft, bounds_upload_adjoint, bounds_upload_fused,
+                  bounds_upload_optim})
+    if ((e = up(t)) != cudaSuccess) return cuda_fail(e, "bounds table upload");
+  return NSGB_OK;
+}
+
+int bounds_add(std::vector<std::pair<unsigned long long, unsigned long long>>& v, const void* p, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_bounds_mu);
+  const unsigned long long a = (unsigned long long)p;
+  v.emplace_back(a, a + bytes);
+  return bounds_upload_locked();
+}
+int bounds_remove(std::vector<std::pair<unsigned long long, unsigned long long>>& v, const void* p) {
+  std::lock_guard<std::mutex> lk(g_bounds_mu);
+  const unsigned long long a = (unsigned long long)p;
+  for (size_t k = 0; k < v.size(); ++k)
+    if (v[k].first == a) {
+      v.erase(v.begin() + k);
+      return bounds_upload_locked();
+    }
+  return NSGB_OK;
+}
+}  // namespace
+#endif
+
+int nsgb::bounds_add_library_range(const void* p, size_t bytes) {
+#ifdef NSGB_CHECK_BOUNDS
+  return bounds_add(g_bounds_lib, p, bytes);
+#else
+  (void)p;
+  (void)bytes;
+  return NSGB_OK;
+#endif
+}
+
+int nsgb::bounds_remove_library_range(const void* p) {
+#ifdef NSGB_CHECK_BOUNDS
+  return bounds_remove(g_bounds_lib, p);
+#else
+  (void)p;
+  return NSGB_OK;
+#endif
+}
+
+int nsgb::finish_call(cudaStream_t st) {
+#ifdef NSGB_CHECK_BOUNDS
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+  if (cap != cudaStreamCaptureStatusNone) return NSGB_OK;  // checked when the graph is launched eagerly
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "bounds check: stream");
+  unsigned long long r[4] = {0, 0, 0, 0};
+  std::lock_guard<std::mutex> lk(g_bounds_mu);
+  if (!g_bounds_report) return NSGB_OK;
+  if ((e = cudaMemcpy(r, g_bounds_report, sizeof r, cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_fail(e, "bounds report");
+  if (r[0] == 0) return NSGB_OK;
+  if ((e = cudaMemset(g_bounds_report, 0, sizeof r)) != cudaSuccess) return cuda_fail(e, "bounds report");
+  return fail(NSGB_ERR_BOUNDS,
+              "out-of-range device access: %llu access(es) outside the valid ranges, the first at address 0x%llx "
+              "(%llu bytes) from translation unit %llu, source line %llu",
+              r[0], r[1], r[3], r[2] / 100000ull, r[2] % 100000ull);
+#else
+  (void)st;
+  return NSGB_OK;
+#endif
+}
+
 cudaError_t nsgb::raise_smem_limit(const void* kernel) {
   static std::mutex mu;
   static std::map<std::pair<const void*, int>, cudaError_t> done;
@@ -608,6 +715,42 @@ extern "C" {
 int nsgb_version(void) { return 10000; }
 
 const char* nsgb_last_error(void) { return g_last_error.c_str(); }
+
+int nsgb_bounds_checking(void) {
+#ifdef NSGB_CHECK_BOUNDS
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+int nsgb_bounds_register(const void* base, size_t bytes) {
+  if (!base || bytes == 0) return fail(NSGB_ERR_INVALID_ARG, "bounds range is empty");
+#ifdef NSGB_CHECK_BOUNDS
+  return bounds_add(g_bounds_caller, base, bytes);
+#else
+  return NSGB_OK;
+#endif
+}
+
+int nsgb_bounds_unregister(const void* base) {
+#ifdef NSGB_CHECK_BOUNDS
+  return bounds_remove(g_bounds_caller, base);
+#else
+  (void)base;
+  return NSGB_OK;
+#endif
+}
+
+int nsgb_bounds_clear(void) {
+#ifdef NSGB_CHECK_BOUNDS
+  std::lock_guard<std::mutex> lk(g_bounds_mu);
+  g_bounds_caller.clear();
+  return bounds_upload_locked();
+#else
+  return NSGB_OK;
+#endif
+}
 
 int nsgb_plan_create(int N, double L, nsgb_plan** out) {
   if (!out) return fail(NSGB_ERR_INVALID_ARG, "out is NULL");
@@ -667,6 +810,8 @@ int nsgb_plan_create(int N, double L, nsgb_plan** out) {
     return fail(e == cudaErrorMemoryAllocation ? NSGB_ERR_OOM : NSGB_ERR_CUDA, "plan set-up: %s",
                 cudaGetErrorString(e));
   }
+  if (int r = bounds_add_library_range(p->tw, ntw * sizeof(float2))) return r;
+  if (int r = bounds_add_library_range(p->k2, N * sizeof(float))) return r;
   *out = p;
   return NSGB_OK;
 }
@@ -679,6 +824,8 @@ int nsgb_plan_destroy(nsgb_plan* plan) {
   if (plan->graph_stream) cudaStreamDestroy(plan->graph_stream);
   if (plan->ev_in) cudaEventDestroy(plan->ev_in);
   if (plan->ev_out) cudaEventDestroy(plan->ev_out);
+  bounds_remove_library_range(plan->tw);
+  bounds_remove_library_range(plan->k2);
   cudaFree(plan->tw);
   cudaFree(plan->k2);
   delete plan;
@@ -810,21 +957,21 @@ int nsgb_grad(const nsgb_plan* plan, const float* f, float* gx, float* gy, void*
   if (int r = check_plan(plan)) return r;
   if (!f || !gx || !gy) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   NSGB_CUDA(launch_grad(f, gx, gy, make_consts(plan, nullptr), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_laplacian(const nsgb_plan* plan, const float* f, float* out, void* stream) {
   if (int r = check_plan(plan)) return r;
   if (!f || !out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   NSGB_CUDA(launch_laplacian(f, out, make_consts(plan, nullptr), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_divergence(const nsgb_plan* plan, const float* u, float* out, void* stream) {
   if (int r = check_plan(plan)) return r;
   if (!u || !out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   NSGB_CUDA(launch_divergence(u, out, make_consts(plan, nullptr), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_advect(const nsgb_plan* plan, int scheme, const float* field, const float* ux, const float* uy,
@@ -834,7 +981,7 @@ int nsgb_advect(const nsgb_plan* plan, int scheme, const float* field, const flo
     return fail(NSGB_ERR_INVALID_ARG, "unknown advection scheme %d", scheme);
   if (!field || !ux || !uy || !out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   NSGB_CUDA(launch_advect(scheme, field, ux, uy, out, make_consts(plan, nullptr), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_poisson(const nsgb_plan* plan, const float* rhs, float* p, void* workspace, size_t ws_bytes,
@@ -843,7 +990,7 @@ int nsgb_poisson(const nsgb_plan* plan, const float* rhs, float* p, void* worksp
   if (!rhs || !p) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   if (int r = check_ws(workspace, ws_bytes, nsgb_poisson_workspace_bytes(plan))) return r;
   NSGB_CUDA(poisson_fft(plan->N, fft_launch(plan, rhs, workspace, p), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_forcing(const nsgb_plan* plan, const nsgb_phys* phys, const float* theta, int theta_len, float t,
@@ -853,7 +1000,7 @@ int nsgb_forcing(const nsgb_plan* plan, const nsgb_phys* phys, const float* thet
   if (int r = check_theta(theta, theta_len)) return r;
   if (!f_out) return fail(NSGB_ERR_INVALID_ARG, "NULL field pointer");
   NSGB_CUDA(launch_forcing_field(theta, theta_len, t, f_out, make_consts(plan, phys), (cudaStream_t)stream));
-  return NSGB_OK;
+  return finish_call((cudaStream_t)stream);
 }
 
 int nsgb_projector_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, const float* f,
@@ -876,7 +1023,7 @@ int nsgb_projector_step(const nsgb_plan* plan, const nsgb_phys* phys, const floa
   NSGB_CUDA(launch_stencil(a, MODE_FIELD, st));
   NSGB_CUDA(poisson_fft(plan->N, fft_launch(plan, w.rhs, w.spec, w.p), st));
   NSGB_CUDA(launch_project(w.usA, w.p, u_out, a.c, st));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 int nsgb_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, const float* theta, int theta_len,
@@ -905,7 +1052,7 @@ int nsgb_step(const nsgb_plan* plan, const nsgb_phys* phys, const float* u, cons
   NSGB_CUDA(launch_stencil(a, MODE_ROLLOUT, st));
   NSGB_CUDA(poisson_fft(plan->N, fft_launch(plan, w.rhs, w.spec, w.p), st));
   NSGB_CUDA(launch_project(w.usA, w.p, u_out, a.c, st));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0, const float* theta,
@@ -938,7 +1085,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
   if (steps == 0) {
     NSGB_CUDA(cudaMemcpyAsync(u_final, u0, 2 * NN * sizeof(float), cudaMemcpyDeviceToDevice, st));
     NSGB_CUDA(launch_jreduce(w.jpart, nblk, 0, w.jsteps, J, 0.0, st));
-    return NSGB_OK;
+    return finish_call(st);
   }
 
   // step 0 reads u0 directly; later steps ping-pong usA <-> usB (and, fused,
@@ -1044,7 +1191,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
   NSGB_CUDA(launch_project(cur, w.p, u_final, a.c, st));
   NSGB_CUDA(launch_jreduce(w.jpart, nblk, steps, w.jsteps, J, (double)phys->dt * (plan->L / plan->N) *
                                                                   (plan->L / plan->N), st));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 }  // extern "C"
@@ -1158,7 +1305,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   NSGB_CUDA(cudaStreamIsCapturing(st, &cap));
   if (cap != cudaStreamCaptureStatusNone)
     return grad_enqueue(plan, phys, u0, theta, theta_len, steps, every, phases, J, u_final, dJdtheta, dJdu0,
-                        workspace, st);
+                        workspace, st);  // (a capture is checked when it runs)
   GradKey key;
   std::memset(&key, 0, sizeof key);
   key.ws = workspace;
@@ -1192,8 +1339,9 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
     std::memcpy(&pl->last_grad, &key, sizeof key);
     if (!repeat) {
       lk.unlock();
-      return grad_enqueue(plan, phys, u0, theta, theta_len, steps, every, phases, J, u_final, dJdtheta, dJdu0,
-                          workspace, st);
+      const int r = grad_enqueue(plan, phys, u0, theta, theta_len, steps, every, phases, J, u_final, dJdtheta,
+                                 dJdu0, workspace, st);
+      return r ? r : finish_call(st);
     }
     if (!pl->graph_stream) {
       NSGB_CUDA(cudaStreamCreateWithFlags(&pl->graph_stream, cudaStreamNonBlocking));
@@ -1224,7 +1372,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
   NSGB_CUDA(cudaGraphLaunch(exec, pl->graph_stream));
   NSGB_CUDA(cudaEventRecord(pl->ev_out, pl->graph_stream));
   NSGB_CUDA(cudaStreamWaitEvent(st, pl->ev_out, 0));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 }  // extern "C"
@@ -1577,7 +1725,7 @@ int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops,
       }
     }
   }
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 // ----------------------------------------------------------- optimiser --
@@ -1708,7 +1856,7 @@ int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void
   std::vector<cudaStream_t> one{st};
   for (int k = 0; k < maxtodo; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
   NSGB_CUDA(ensemble_finalize(members, order, tab, steps, (SolveDev*)(base + L.fin_off), st));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, void* workspace, size_t ws_bytes,
@@ -1801,7 +1949,7 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
   }
   for (int k = 0; k < steps - s; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
   NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + L.fin_off), st));
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta,
@@ -1884,7 +2032,7 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return cuda_fail(err, "nsgb_time_stages");
   for (int k = 0; k < 4; ++k) out_ms[k] = (float)(tot[k] / reps);
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const float* u0, const float* theta,
@@ -1971,7 +2119,7 @@ int nsgb_time_step_pipeline(const nsgb_plan* plan, const nsgb_phys* phys, const 
     if (e) cudaEventDestroy(e);
   if (err != cudaSuccess) return cuda_fail(err, "nsgb_time_step_pipeline");
   for (int k = 0; k < 4; ++k) out_ms[k] = (float)(tot[k] / steps);
-  return NSGB_OK;
+  return finish_call(st);
 }
 
 }  // extern "C"

@@ -14,6 +14,91 @@
 
 namespace nsgb {
 
+// ------------------------------------------------------ bounds checking --
+// Every global-memory access of the kernels goes through the accessors below.
+// In the bounds-checking build (compiled with NSGB_CHECK_BOUNDS) each access
+// is checked against the device ranges the library knows to be valid (the
+// plans' tables, the no-allocation scratch, and the ranges the caller
+// registered with nsgb_bounds_register); an access outside all of them is
+// skipped (a load yields zero) and recorded, and the entry point returns
+// NSGB_ERR_BOUNDS instead of faulting.  In the normal build the accessors are
+// the plain accesses.
+namespace bounds {
+constexpr int kMaxRanges = 96;
+struct Table {
+  int n;
+  int unit;                                  // translation unit of this copy (reported with the line)
+  unsigned long long lo[kMaxRanges];         // [lo, hi) byte ranges
+  unsigned long long hi[kMaxRanges];
+  unsigned long long* report;                // device: count, first address, unit*100000+line, bytes
+};
+}  // namespace bounds
+
+#ifdef NSGB_CHECK_BOUNDS
+// One copy per translation unit, set by that unit's bounds_upload_<unit>.
+static __constant__ bounds::Table g_bounds;
+
+__device__ __noinline__ static void bounds_record(unsigned long long a, unsigned bytes, int line) {
+  unsigned long long* r = g_bounds.report;
+  if (!r) return;
+  if (atomicAdd(r, 1ull) == 0ull) {
+    r[1] = a;
+    r[2] = (unsigned long long)g_bounds.unit * 100000ull + (unsigned long long)line;
+    r[3] = bytes;
+  }
+}
+__device__ __forceinline__ bool bounds_ok(const void* p, unsigned bytes, int line) {
+  const unsigned long long a = (unsigned long long)p;
+  for (int k = 0; k < g_bounds.n; ++k)
+    if (a >= g_bounds.lo[k] && a + bytes <= g_bounds.hi[k]) return true;
+  bounds_record(a, bytes, line);
+  return false;
+}
+// Defines the host function that uploads a table to this unit's copy.
+#define NSGB_BOUNDS_UNIT(name, id)                                                   \
+  cudaError_t bounds_upload_##name(const bounds::Table& t) {                         \
+    bounds::Table u = t;                                                              \
+    u.unit = (id);                                                                    \
+    return cudaMemcpyToSymbol(g_bounds, &u, sizeof u);                                \
+  }
+#else
+__device__ __forceinline__ bool bounds_ok(const void*, unsigned, int) { return true; }
+#define NSGB_BOUNDS_UNIT(name, id)
+#endif
+
+// Plain load / store.
+template <class T>
+__device__ __forceinline__ T gld(const T* p, int line = __builtin_LINE()) {
+  return bounds_ok(p, sizeof(T), line) ? *p : T{};
+}
+template <class T>
+__device__ __forceinline__ void gst(T* p, T v, int line = __builtin_LINE()) {
+  if (bounds_ok(p, sizeof(T), line)) *p = v;
+}
+// Read-only-path load (__ldg), streaming load and store (__ldcs, __stcs).
+template <class T>
+__device__ __forceinline__ T gldg(const T* p, int line = __builtin_LINE()) {
+  return bounds_ok(p, sizeof(T), line) ? __ldg(p) : T{};
+}
+template <class T>
+__device__ __forceinline__ T gldcs(const T* p, int line = __builtin_LINE()) {
+  return bounds_ok(p, sizeof(T), line) ? __ldcs(p) : T{};
+}
+template <class T>
+__device__ __forceinline__ void gstcs(T* p, T v, int line = __builtin_LINE()) {
+  if (bounds_ok(p, sizeof(T), line)) __stcs(p, v);
+}
+// float4 views of float arrays (16-byte aligned offsets).
+__device__ __forceinline__ float4 gldg4(const float* p, int line = __builtin_LINE()) {
+  return gldg(reinterpret_cast<const float4*>(p), line);
+}
+__device__ __forceinline__ float4 gld4(const float* p, int line = __builtin_LINE()) {
+  return gld(reinterpret_cast<const float4*>(p), line);
+}
+__device__ __forceinline__ void gst4(float* p, float4 v, int line = __builtin_LINE()) {
+  gst(reinterpret_cast<float4*>(p), v, line);
+}
+
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }

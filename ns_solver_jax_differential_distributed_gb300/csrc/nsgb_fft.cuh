@@ -196,7 +196,7 @@ __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, in
       // twiddle loads instead of 15
       const int bm = b & (NS - 1);
       const float2* __restrict__ tp = tw + tw_offset<E>(NS) + bm;
-      float2 w1 = __ldg(tp + NS), w2 = __ldg(tp + 2 * NS), w4 = __ldg(tp + 4 * NS), w8 = __ldg(tp + 8 * NS);
+      float2 w1 = gldg(tp + NS), w2 = gldg(tp + 2 * NS), w4 = gldg(tp + 4 * NS), w8 = gldg(tp + 8 * NS);
       if (INV) {
         w1.y = -w1.y;
         w2.y = -w2.y;
@@ -224,7 +224,7 @@ __device__ __forceinline__ void pass(float2 (&a)[E], float2* __restrict__ sb, in
       const float2* __restrict__ tp = tw + tw_offset<E>(NS) + bm;
 #pragma unroll
       for (int r = 1; r < RP; ++r) {
-        float2 w = __ldg(tp + r * NS);
+        float2 w = gldg(tp + r * NS);
         if (INV) w.y = -w.y;
         x[r] = cmul(x[r], w);
       }

@@ -52,7 +52,7 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
   // Row data is read once: evict-first loads keep the twiddle tables in L1.
   float2 a[E];
 #pragma unroll
-  for (int s = 0; s < E; ++s) a[s] = make_float2(__ldcs(ra + j + s * T), __ldcs(rb + j + s * T));
+  for (int s = 0; s < E; ++s) a[s] = make_float2(gldcs(ra + j + s * T), gldcs(rb + j + s * T));
   fft::block_fft<N, false, E>(a, sb, j, tw);
   __syncthreads();
   fft::store_strided<T, E>(a, sb, j);
@@ -71,8 +71,8 @@ __device__ __forceinline__ void rows_fwd_body(const float* __restrict__ rhs, flo
     const int k = e >> lp;
     const float2* pb = smem2 + q * pair_stride<N>();
     const float2 zk = pb[pad(k)], wk = pb[pad((N - k) & (N - 1))];
-    *reinterpret_cast<float4*>(spec + (size_t)k * N + i0 + 2 * q) =
-        make_float4(zk.x + wk.x, zk.y - wk.y, zk.y + wk.y, wk.x - zk.x);
+    gst(reinterpret_cast<float4*>(spec + (size_t)k * N + i0 + 2 * q),
+        make_float4(zk.x + wk.x, zk.y - wk.y, zk.y + wk.y, wk.x - zk.x));
   }
 }
 
@@ -102,20 +102,20 @@ __device__ __forceinline__ void cols_body(float2* __restrict__ spec, const float
 
   float2 a[E];
 #pragma unroll
-  for (int s = 0; s < E; ++s) a[s] = __ldcs(row + j + s * T);
+  for (int s = 0; s < E; ++s) a[s] = gldcs(row + j + s * T);
   fft::block_fft<N, false, E>(a, sb, j, tw);
 
-  const float k2y = __ldg(k2 + ky);
+  const float k2y = gldg(k2 + ky);
 #pragma unroll
   for (int s = 0; s < E; ++s) {
-    const float g = poisson_mult(__ldg(k2 + j + s * T), k2y, scale);
+    const float g = poisson_mult(gldg(k2 + j + s * T), k2y, scale);
     a[s] = make_float2(a[s].x * g, a[s].y * g);
   }
   fft::block_fft<N, true, E>(a, sb, j, tw);
   __syncthreads();  // rows clamped to N/2 were loaded by other threads
   if (kreq <= H) {
 #pragma unroll
-    for (int s = 0; s < E; ++s) row[j + s * T] = a[s];
+    for (int s = 0; s < E; ++s) gst(row + j + s * T, a[s]);
   }
 }
 
@@ -162,11 +162,11 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
     for (; e + 7 * nth < tot; e += 8 * nth) {
       float4 v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = __ldcs(src(e + u * nth));
+      for (int u = 0; u < 8; ++u) v[u] = gldcs(src(e + u * nth));
 #pragma unroll
       for (int u = 0; u < 8; ++u) stage(e + u * nth, v[u]);
     }
-    for (; e < tot; e += nth) stage(e, __ldcs(src(e)));
+    for (; e < tot; e += nth) stage(e, gldcs(src(e)));
   }
   __syncthreads();
 
@@ -179,8 +179,8 @@ __device__ __forceinline__ void rows_inv_body(const float2* __restrict__ spec, f
   float* rb = ra + N;
 #pragma unroll
   for (int s = 0; s < E; ++s) {
-    ra[j + s * T] = a[s].x;
-    rb[j + s * T] = a[s].y;
+    gst(ra + j + s * T, a[s].x);
+    gst(rb + j + s * T, a[s].y);
   }
 }
 
@@ -319,5 +319,7 @@ cudaError_t poisson_fft(int N, const FftLaunch& L, cudaStream_t st) { return dis
 cudaError_t poisson_fft_batch(int N, const FftLaunch& L, const SolveDev* solves, int count, cudaStream_t st) {
   return dispatch(N, L, solves, count, st);
 }
+
+NSGB_BOUNDS_UNIT(fft, 2)
 
 }  // namespace nsgb

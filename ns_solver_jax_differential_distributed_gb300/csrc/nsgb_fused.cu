@@ -143,9 +143,9 @@ __device__ __forceinline__ void inverse_pair(const float2* __restrict__ spec, in
   const int ir = i & (N - 1);
   float4 v[U];
 #pragma unroll
-  for (int u = 0; u < U; ++u) v[u] = __ldg(reinterpret_cast<const float4*>(spec + (size_t)(j + u * T) * N + ir));
+  for (int u = 0; u < U; ++u) v[u] = gldg(reinterpret_cast<const float4*>(spec + (size_t)(j + u * T) * N + ir));
   float4 vh = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (j == 0) vh = __ldg(reinterpret_cast<const float4*>(spec + (size_t)H * N + ir));
+  if (j == 0) vh = gldg(reinterpret_cast<const float4*>(spec + (size_t)H * N + ir));
   // X_a[k] = (x, y), X_b[k] = (z, w):  Z[k] = X_a + i X_b,  Z[N-k] = conj(X_a) + i conj(X_b);
   // DC and Nyquist keep only the real parts (as Re(ifft2) drops the rest)
 #pragma unroll
@@ -207,8 +207,8 @@ __device__ __forceinline__ void forward_pair(float2* stg, float2* __restrict__ s
   // 2 X_i[k] = Z[k] + conj(Z[N-k]);  2 X_{i+1}[k] = -i (Z[k] - conj(Z[N-k]))
   for (int k = j; k <= H; k += T) {
     const float2 zk = stg[pad(k)], wk = stg[pad((N - k) & (N - 1))];
-    *reinterpret_cast<float4*>(spec + (size_t)k * N + i) =
-        make_float4(zk.x + wk.x, zk.y - wk.y, zk.y + wk.y, wk.x - zk.x);
+    gst(reinterpret_cast<float4*>(spec + (size_t)k * N + i),
+        make_float4(zk.x + wk.x, zk.y - wk.y, zk.y + wk.y, wk.x - zk.x));
   }
 }
 
@@ -248,9 +248,9 @@ __device__ __forceinline__ void fused_rows_body(const FusedArgs& fa) {
   float* sRed = sm + S::RED_OFF;
   float* sF = sm + S::F_OFF;
 
-  const int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed;
+  const int step = (a.step_ctr ? gld(a.step_ctr) : 0) + a.step_fixed;
   const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
-  const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float nu = (a.theta != nullptr && a.theta_len == 3) ? gldg(a.theta + 2) : c.nu;
   const float cL = fmul(c.dtdx2, nu);
 
   // ---- stencil role state
@@ -426,7 +426,7 @@ __device__ __forceinline__ void fused_rows_body(const FusedArgs& fa) {
 
   // ---- stencil role: prologue (forcing rows, the first u* rows)
   {
-    const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t_now, c);
+    const ForcingRow fr = forcing_time(gldg(a.theta), gldg(a.theta + 1), t_now, c);
     for (int k = tid; k < r1 - r0 + 2; k += ST) sF[k] = forcing_fx((r0 - 1 + k) & M, fr, c);
     for (int k = tid; k < 12 * NWS; k += ST) sE[k] = 0.0f;
 #pragma unroll
@@ -453,7 +453,7 @@ __device__ __forceinline__ void fused_rows_body(const FusedArgs& fa) {
     v = warp_sum(v);
     if (lane == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
       const int nblk = gridDim.x * gridDim.y;
-      a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+      gst(a.jpart + (size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x, v);
     }
   }
 }
@@ -534,5 +534,7 @@ cudaError_t fused_default_rows(int N, int& rows) {
   if (rows < 2) rows = 2;
   return cudaSuccess;
 }
+
+NSGB_BOUNDS_UNIT(fused, 4)
 
 }  // namespace nsgb

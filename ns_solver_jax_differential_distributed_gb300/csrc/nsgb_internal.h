@@ -177,6 +177,14 @@ void set_last_error(const char* msg);
 // kernel with different sizes from several host threads cannot race on the
 // limit.
 cudaError_t raise_smem_limit(const void* kernel);
+// Bounds-checking build: a device range of the library's own (plan tables,
+// static scratch) that kernels may access; no-op otherwise.
+int bounds_add_library_range(const void* p, size_t bytes);
+int bounds_remove_library_range(const void* p);
+// The status an entry point returns after enqueueing its work: NSGB_OK, or
+// in the bounds-checking build NSGB_ERR_BOUNDS when a kernel of the call
+// accessed memory outside the valid ranges (it waits for the stream).
+int finish_call(cudaStream_t st);
 template <class K>
 inline cudaError_t raise_smem_limit(K* kernel) {
   return raise_smem_limit(reinterpret_cast<const void*>(kernel));

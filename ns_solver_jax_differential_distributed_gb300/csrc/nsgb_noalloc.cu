@@ -122,6 +122,10 @@ extern "C" int nsgb_poisson_noalloc(int N, double L, const float* rhs, float* p,
     if ((e = cudaGetSymbolAddress(&a, g_noalloc_k2)) != cudaSuccess)
       return fail(NSGB_ERR_CUDA, "cudaGetSymbolAddress(k2): %s", cudaGetErrorString(e));
     d.k2 = (float*)a;
+    int r = nsgb::bounds_add_library_range(d.spec, sizeof g_noalloc_spec);
+    if (!r) r = nsgb::bounds_add_library_range(d.tw, sizeof g_noalloc_tw);
+    if (!r) r = nsgb::bounds_add_library_range(d.k2, sizeof g_noalloc_k2);
+    if (r) return r;
     d.ready = true;
   }
   fill_tables(N, L);
@@ -145,5 +149,5 @@ extern "C" int nsgb_poisson_noalloc(int N, double L, const float* rhs, float* p,
   Lc.cols_per_cta = 1;
   e = nsgb::poisson_fft(N, Lc, st);
   if (e != cudaSuccess) return fail(NSGB_ERR_CUDA, "poisson kernels: %s", cudaGetErrorString(e));
-  return NSGB_OK;
+  return nsgb::finish_call(st);
 }

@@ -19,26 +19,26 @@ __global__ void k_optimizer_update(OptimizerRule r, float* __restrict__ theta,
                                    float* __restrict__ nu, float* __restrict__ theta_copy, int n) {
   const int k = threadIdx.x;
   if (k >= n) return;
-  const float g = grad[k];
+  const float g = gld(grad + k);
   float u;
   if (r.kind == NSGB_OPT_SGD) {
     u = __fmul_rn(g, -r.lr);
   } else if (r.kind == NSGB_OPT_ADAM) {
-    const float m = __fadd_rn(__fmul_rn(r.one_minus_b1, g), __fmul_rn(r.b1, mu[k]));
-    const float v = __fadd_rn(__fmul_rn(r.one_minus_b2, __fmul_rn(g, g)), __fmul_rn(r.b2, nu[k]));
-    mu[k] = m;
-    nu[k] = v;
+    const float m = __fadd_rn(__fmul_rn(r.one_minus_b1, g), __fmul_rn(r.b1, gld(mu + k)));
+    const float v = __fadd_rn(__fmul_rn(r.one_minus_b2, __fmul_rn(g, g)), __fmul_rn(r.b2, gld(nu + k)));
+    gst(mu + k, m);
+    gst(nu + k, v);
     const float m_hat = __fdiv_rn(m, r.bc1);
     const float v_hat = __fdiv_rn(v, r.bc2);
     u = __fmul_rn(__fdiv_rn(m_hat, __fadd_rn(__fsqrt_rn(__fadd_rn(v_hat, r.eps_root)), r.eps)), -r.lr);
   } else {
-    const float v = __fadd_rn(__fmul_rn(r.one_minus_decay, __fmul_rn(g, g)), __fmul_rn(r.decay, nu[k]));
-    nu[k] = v;
+    const float v = __fadd_rn(__fmul_rn(r.one_minus_decay, __fmul_rn(g, g)), __fmul_rn(r.decay, gld(nu + k)));
+    gst(nu + k, v);
     u = __fmul_rn(__fmul_rn(g, rsqrtf(__fadd_rn(v, r.eps))), -r.lr);
   }
-  const float t = __fadd_rn(theta[k], u);
-  theta[k] = t;
-  if (theta_copy) theta_copy[k] = t;
+  const float t = __fadd_rn(gld(theta + k), u);
+  gst(theta + k, t);
+  if (theta_copy) gst(theta_copy + k, t);
 }
 
 cudaError_t launch_optimizer_update(const OptimizerRule& r, float* theta, const float* grad, float* mu,
@@ -46,5 +46,7 @@ cudaError_t launch_optimizer_update(const OptimizerRule& r, float* theta, const 
   k_optimizer_update<<<1, 32, 0, st>>>(r, theta, grad, mu, nu, theta_copy, n);
   return cudaGetLastError();
 }
+
+NSGB_BOUNDS_UNIT(optim, 5)
 
 }  // namespace nsgb

@@ -31,7 +31,8 @@ __device__ __forceinline__ uint64_t evict_first_policy() {
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
   return pol;
 }
-__device__ __forceinline__ void cp16(float* dst_smem, const float* src, uint64_t pol) {
+__device__ __forceinline__ void cp16(float* dst_smem, const float* src, uint64_t pol, int line = __builtin_LINE()) {
+  if (!bounds_ok(src, 16, line)) return;
   asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;" ::"r"(
                    (unsigned)__cvta_generic_to_shared(dst_smem)),
                "l"(src), "l"(pol)
@@ -59,7 +60,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* mb, unsigned bytes) {
 }
 // `bytes` (a multiple of 16, both addresses 16-byte aligned) from global src
 // to this CTA's shared dst; completes `bytes` transactions on mb.
-__device__ __forceinline__ void bulk_g2s(float* dst, const float* src, unsigned bytes, uint64_t* mb, uint64_t pol) {
+__device__ __forceinline__ void bulk_g2s(float* dst, const float* src, unsigned bytes, uint64_t* mb, uint64_t pol,
+                                         int line = __builtin_LINE()) {
+  if (!bounds_ok(src, bytes, line)) return;  // the mbarrier's wait then runs out (bounded)
   asm volatile(
       "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
           "r"(smem_u32(dst)),
@@ -112,13 +115,15 @@ __device__ __forceinline__ RowPieces row_pieces(int N, int W, int j0) {
   return r;
 }
 
-__device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4]) {
-  *reinterpret_cast<float4*>(base + off) = make_float4(v[0], v[1], v[2], v[3]);
+__device__ __forceinline__ void st4(float* __restrict__ base, size_t off, const float (&v)[4],
+                                    int line = __builtin_LINE()) {
+  gst4(base + off, make_float4(v[0], v[1], v[2], v[3]), line);
 }
 // Evict-first store, for fields read only after the FFT passes (u*next), so
 // they do not push the passes' inputs out of L2.
-__device__ __forceinline__ void st4_stream(float* __restrict__ base, size_t off, const float (&v)[4]) {
-  __stcs(reinterpret_cast<float4*>(base + off), make_float4(v[0], v[1], v[2], v[3]));
+__device__ __forceinline__ void st4_stream(float* __restrict__ base, size_t off, const float (&v)[4],
+                                           int line = __builtin_LINE()) {
+  gstcs(reinterpret_cast<float4*>(base + off), make_float4(v[0], v[1], v[2], v[3]), line);
 }
 __device__ __forceinline__ void ld4s(const float* s, float (&o)[4]) {
   const float4 v = *reinterpret_cast<const float4*>(s);
@@ -132,11 +137,12 @@ __device__ __forceinline__ void ld4s(const float* s, float (&o)[4]) {
 // into a ring row: thread g copies its group's four columns, and for W = N
 // the first and last threads also copy the wrapped neighbours.
 __device__ __forceinline__ void copy_row(float* ring_row, const float* __restrict__ field, int row, int N, int M,
-                                         bool wrap, bool active, int tid, int G, int bi, int col, uint64_t pol) {
+                                         bool wrap, bool active, int tid, int G, int bi, int col, uint64_t pol,
+                                         int line = __builtin_LINE()) {
   const float* src = field + (size_t)(row & M) * N;
-  if (active) cp16(ring_row + bi, src + col, pol);
-  if (wrap && tid == 0) cp16(ring_row + 4, src + N - 4, pol);
-  if (wrap && tid == G - 1) cp16(ring_row + N + 8, src, pol);
+  if (active) cp16(ring_row + bi, src + col, pol, line);
+  if (wrap && tid == 0) cp16(ring_row + 4, src + N - 4, pol, line);
+  if (wrap && tid == G - 1) cp16(ring_row + N + 8, src, pol, line);
 }
 
 }  // namespace rows

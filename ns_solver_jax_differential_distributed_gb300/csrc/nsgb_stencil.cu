@@ -63,10 +63,10 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   int step = 0;
   float t = a.t_fixed;
   if (MODE == MODE_ROLLOUT) {
-    step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
+    step = (a.step_ctr ? gld(a.step_ctr) : 0) + a.step_fixed + step_off;
     if (a.t_from_step) t = fmul((float)step, c.dt);
   }
-  const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float nu = (a.theta != nullptr && a.theta_len == 3) ? gldg(a.theta + 2) : c.nu;
   const float cL = fmul(c.dtdx2, nu);
 
   // Tile loads: aligned float4 groups (a group never straddles the periodic
@@ -75,8 +75,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
   if (has_p) {
     const float* __restrict__ pp = a.p;
     forflat<PH, G>(tid, [&](int r, int q) {
-      const float4 v = __ldg(reinterpret_cast<const float4*>(
-          pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M)));
+      const float4 v = gldg4(pp + (size_t)((i0 - 3 + r) & M) * N + ((j0 - 4 + 4 * q) & M));
       *reinterpret_cast<float4*>(sP + r * W4 + 4 * q) = v;
     });
   }
@@ -84,12 +83,12 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     const float* __restrict__ us = a.us;
     forflat<UH, G>(tid, [&](int r, int q) {
       const size_t g = (size_t)((i0 - 2 + r) & M) * N + ((j0 - 4 + 4 * q) & M);
-      *reinterpret_cast<float4*>(sUx + r * W4 + 4 * q) = __ldg(reinterpret_cast<const float4*>(us + g));
-      *reinterpret_cast<float4*>(sUy + r * W4 + 4 * q) = __ldg(reinterpret_cast<const float4*>(us + NN + g));
+      *reinterpret_cast<float4*>(sUx + r * W4 + 4 * q) = gldg4(us + g);
+      *reinterpret_cast<float4*>(sUy + r * W4 + 4 * q) = gldg4(us + NN + g);
     });
   }
   if (MODE == MODE_ROLLOUT && tid < SH) {
-    const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t, c);
+    const ForcingRow fr = forcing_time(gldg(a.theta), gldg(a.theta + 1), t, c);
     sF[tid] = forcing_fx((i0 - 1 + tid) & M, fr, c);
   }
   __syncthreads();
@@ -114,8 +113,8 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     if (MODE == MODE_ROLLOUT) jacc += sUx[o] * sF[r + 1];
     if (a.u_out) {
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      a.u_out[g] = sUx[o];
-      a.u_out[NN + g] = sUy[o];
+      gst(a.u_out + g, sUx[o]);
+      gst(a.u_out + NN + g, sUy[o]);
     }
   });
 
@@ -143,8 +142,8 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
         fy = 0.0f;
       } else {
         const size_t g = (size_t)((i0 - 1 + r + k) & M) * N + ((j0 - 1 + cc) & M);
-        fx = __ldg(a.f + g);
-        fy = __ldg(a.f + NN + g);
+        fx = gldg(a.f + g);
+        fy = gldg(a.f + NN + g);
       }
       const int so = (r + k) * SW + cc;
       sSx[so] = fused_ustar<SCHEME>(ox, lx, rx, ux_, dx_, ox, oy, cL, fmul(c.dt, fx), c);
@@ -160,9 +159,9 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
     forflat<TH, TW>(tid, [&](int r, int cc) {
       const int o = (r + 1) * SW + cc + 1;
       const size_t g = (size_t)(i0 + r) * N + (j0 + cc);
-      uso[g] = sSx[o];
-      uso[NN + g] = sSy[o];
-      rhs[g] = fused_rhs(sSx[o + SW], sSx[o - SW], sSy[o + 1], sSy[o - 1], c.cD);
+      gst(uso + g, sSx[o]);
+      gst(uso + NN + g, sSy[o]);
+      gst(rhs + g, fused_rhs(sSx[o + SW], sSx[o - SW], sSy[o + 1], sSy[o - 1], c.cD));
     });
   }
 
@@ -176,7 +175,7 @@ __device__ __forceinline__ void stencil_body(const StencilArgs& a, int step_off 
       v = warp_sum(v);
       if (tx == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
         const int nblk = gridDim.x * gridDim.y;
-        a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+        gst(a.jpart + (size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x, v);
       }
     }
   }
@@ -285,12 +284,12 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
   // r0-3, r0-2
   uint64_t* sMb = reinterpret_cast<uint64_t*>(sm + (((kPRing + 2 * kURing) * (size_t)RS + (size_t)12 * G + RH + 2 + 32 + 1) & ~(size_t)1));
 
-  int step = (a.step_ctr ? *a.step_ctr : 0) + a.step_fixed + step_off;
+  int step = (a.step_ctr ? gld(a.step_ctr) : 0) + a.step_fixed + step_off;
   const float t_now = a.t_from_step ? fmul((float)step, c.dt) : a.t_fixed;
-  const float nu = (a.theta != nullptr && a.theta_len == 3) ? __ldg(a.theta + 2) : c.nu;
+  const float nu = (a.theta != nullptr && a.theta_len == 3) ? gldg(a.theta + 2) : c.nu;
   const float cL = fmul(c.dtdx2, nu);
   {
-    const ForcingRow fr = forcing_time(__ldg(a.theta), __ldg(a.theta + 1), t_now, c);
+    const ForcingRow fr = forcing_time(gldg(a.theta), gldg(a.theta + 1), t_now, c);
     for (int k = tid; k < r1 - r0 + 2; k += blockDim.x) sF[k] = forcing_fx((r0 - 1 + k) & M, fr, c);
   }
 
@@ -493,7 +492,7 @@ __device__ __forceinline__ void stencil_rows_body(const StencilArgs& a, int step
     if (aborted) v = __int_as_float(0x7fc00000);  // NaN: the step did not complete
     if (lane == 0 && (unsigned)step < (unsigned)a.jpart_rows) {
       const int nblk = gridDim.x * gridDim.y;
-      a.jpart[(size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x] = v;
+      gst(a.jpart + (size_t)step * nblk + blockIdx.y * gridDim.x + blockIdx.x, v);
     }
   }
 }
@@ -651,10 +650,10 @@ __global__ void k_project(const float* __restrict__ us, const float* __restrict_
   const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
-  u[g] = fused_proj(__ldg(us + g), __ldg(p + (size_t)((i + 1) & M) * N + j),
-                    __ldg(p + (size_t)((i - 1) & M) * N + j), c.cP);
-  u[NN + g] = fused_proj(__ldg(us + NN + g), __ldg(p + (size_t)i * N + ((j + 1) & M)),
-                         __ldg(p + (size_t)i * N + ((j - 1) & M)), c.cP);
+  gst(u + g, fused_proj(gldg(us + g), gldg(p + (size_t)((i + 1) & M) * N + j),
+                        gldg(p + (size_t)((i - 1) & M) * N + j), c.cP));
+  gst(u + NN + g, fused_proj(gldg(us + NN + g), gldg(p + (size_t)i * N + ((j + 1) & M)),
+                             gldg(p + (size_t)i * N + ((j - 1) & M)), c.cP));
 }
 
 cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
@@ -674,10 +673,10 @@ __global__ void k_project_batch(const SolveDev* __restrict__ solves, int variant
   if (g >= NN) return;
   const int i = (int)(g >> c.logN), j = (int)(g & M);
   const float* p = a.p;
-  d.u_final[g] = fused_proj(__ldg(a.us + g), __ldg(p + (size_t)((i + 1) & M) * N + j),
-                            __ldg(p + (size_t)((i - 1) & M) * N + j), c.cP);
-  d.u_final[NN + g] = fused_proj(__ldg(a.us + NN + g), __ldg(p + (size_t)i * N + ((j + 1) & M)),
-                                 __ldg(p + (size_t)i * N + ((j - 1) & M)), c.cP);
+  gst(d.u_final + g, fused_proj(gldg(a.us + g), gldg(p + (size_t)((i + 1) & M) * N + j),
+                                gldg(p + (size_t)((i - 1) & M) * N + j), c.cP));
+  gst(d.u_final + NN + g, fused_proj(gldg(a.us + NN + g), gldg(p + (size_t)i * N + ((j + 1) & M)),
+                                     gldg(p + (size_t)i * N + ((j - 1) & M)), c.cP));
 }
 
 // Projection of the final state of every solve: `variant` names the argument
@@ -694,21 +693,21 @@ __global__ void k_jreduce(const float* __restrict__ jpart, int nblk, double* __r
   __shared__ double red[256];
   const float* row = jpart + (size_t)blockIdx.x * nblk;
   double v = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)row[b];
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)gld(row + b);
   red[threadIdx.x] = v;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) jsteps[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) gst(jsteps + blockIdx.x, red[0]);
 }
 
 __global__ void k_jfinal(const double* __restrict__ jsteps, int steps, double jscale,
                          float* __restrict__ J) {
   double acc = 0.0;
-  for (int s = 0; s < steps; ++s) acc += jsteps[s] * jscale;
-  *J = (float)acc;
+  for (int s = 0; s < steps; ++s) acc += gld(jsteps + s) * jscale;
+  gst(J, (float)acc);
 }
 
 cudaError_t launch_jreduce(const float* jpart, int nblk, int steps, double* jsteps, float* J,
@@ -723,14 +722,14 @@ __global__ void k_jreduce_batch(const SolveDev* __restrict__ solves, int nblk) {
   const SolveDev& d = solves[blockIdx.y];
   const float* row = d.st[1].jpart + (size_t)blockIdx.x * nblk;
   double v = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)row[b];
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += (double)gld(row + b);
   red[threadIdx.x] = v;
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x == 0) d.jsteps[blockIdx.x] = red[0];
+  if (threadIdx.x == 0) gst(d.jsteps + blockIdx.x, red[0]);
 }
 
 __global__ void k_jfinal_batch(const SolveDev* __restrict__ solves, int count, int steps) {
@@ -738,8 +737,8 @@ __global__ void k_jfinal_batch(const SolveDev* __restrict__ solves, int count, i
   if (k >= count) return;
   const SolveDev& d = solves[k];
   double acc = 0.0;
-  for (int s = 0; s < steps; ++s) acc += d.jsteps[s] * d.jscale;
-  *d.J = (float)acc;
+  for (int s = 0; s < steps; ++s) acc += gld(d.jsteps + s) * d.jscale;
+  gst(d.J, (float)acc);
 }
 
 cudaError_t launch_jreduce_batch(const SolveDev* solves, int count, int nblk, int steps, cudaStream_t st) {
@@ -752,7 +751,7 @@ __global__ void k_counter_batch(const SolveDev* __restrict__ solves, int count, 
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   int* ctr = solves[k].ctr;
-  *ctr = add ? *ctr + value : solves[k].ctr_init + value;
+  gst(ctr, add ? gld(ctr) + value : solves[k].ctr_init + value);
 }
 
 cudaError_t launch_counter_batch(const SolveDev* solves, int count, int value, bool add, cudaStream_t st) {
@@ -760,7 +759,7 @@ cudaError_t launch_counter_batch(const SolveDev* solves, int count, int value, b
   return cudaGetLastError();
 }
 
-__global__ void k_step_counter(int* ctr, int value, int add) { *ctr = add ? *ctr + value : value; }
+__global__ void k_step_counter(int* ctr, int value, int add) { gst(ctr, add ? gld(ctr) + value : value); }
 cudaError_t launch_step_counter(int* step_ctr, int value, bool add, cudaStream_t st) {
   k_step_counter<<<1, 1, 0, st>>>(step_ctr, value, add ? 1 : 0);
   return cudaGetLastError();
@@ -780,8 +779,8 @@ __global__ void k_grad(const float* __restrict__ f, float* __restrict__ gx, floa
   int i, j;
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
-  gx[g] = divc(fsub(f[(size_t)((i + 1) & M) * N + j], f[(size_t)((i - 1) & M) * N + j]), c.h2, c.rh2);
-  gy[g] = divc(fsub(f[(size_t)i * N + ((j + 1) & M)], f[(size_t)i * N + ((j - 1) & M)]), c.h2, c.rh2);
+  gst(gx + g, divc(fsub(gld(f + (size_t)((i + 1) & M) * N + j), gld(f + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2));
+  gst(gy + g, divc(fsub(gld(f + (size_t)i * N + ((j + 1) & M)), gld(f + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2));
 }
 
 __global__ void k_laplacian(const float* __restrict__ f, float* __restrict__ out, const StepConsts c) {
@@ -791,9 +790,9 @@ __global__ void k_laplacian(const float* __restrict__ f, float* __restrict__ out
   int i, j;
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
-  const float left = f[(size_t)((i - 1) & M) * N + j], right = f[(size_t)((i + 1) & M) * N + j];
-  const float up = f[(size_t)i * N + ((j + 1) & M)], down = f[(size_t)i * N + ((j - 1) & M)];
-  out[g] = divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, f[g])), c.dx2, c.rdx2);
+  const float left = gld(f + (size_t)((i - 1) & M) * N + j), right = gld(f + (size_t)((i + 1) & M) * N + j);
+  const float up = gld(f + (size_t)i * N + ((j + 1) & M)), down = gld(f + (size_t)i * N + ((j - 1) & M));
+  gst(out + g, divc(fsub(fadd(fadd(fadd(left, right), up), down), fmul(4.0f, gld(f + g))), c.dx2, c.rdx2));
 }
 
 __global__ void k_divergence(const float* __restrict__ u, float* __restrict__ out, const StepConsts c) {
@@ -804,9 +803,9 @@ __global__ void k_divergence(const float* __restrict__ u, float* __restrict__ ou
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
   const float* uy = u + NN;
-  const float gx = divc(fsub(u[(size_t)((i + 1) & M) * N + j], u[(size_t)((i - 1) & M) * N + j]), c.h2, c.rh2);
-  const float gy = divc(fsub(uy[(size_t)i * N + ((j + 1) & M)], uy[(size_t)i * N + ((j - 1) & M)]), c.h2, c.rh2);
-  out[g] = fadd(gx, gy);
+  const float gx = divc(fsub(gld(u + (size_t)((i + 1) & M) * N + j), gld(u + (size_t)((i - 1) & M) * N + j)), c.h2, c.rh2);
+  const float gy = divc(fsub(gld(uy + (size_t)i * N + ((j + 1) & M)), gld(uy + (size_t)i * N + ((j - 1) & M))), c.h2, c.rh2);
+  gst(out + g, fadd(gx, gy));
 }
 
 template <int SCHEME>
@@ -818,18 +817,18 @@ __global__ void k_advect(const float* __restrict__ fld, const float* __restrict_
   int i, j;
   ij_of(g, c, i, j);
   const int N = c.N, M = N - 1;
-  const float f = fld[g];
-  const float left = fld[(size_t)((i - 1) & M) * N + j], right = fld[(size_t)((i + 1) & M) * N + j];
-  const float up = fld[(size_t)i * N + ((j + 1) & M)], down = fld[(size_t)i * N + ((j - 1) & M)];
-  const float vx = ux[g], vy = uy[g];
+  const float f = gld(fld + g);
+  const float left = gld(fld + (size_t)((i - 1) & M) * N + j), right = gld(fld + (size_t)((i + 1) & M) * N + j);
+  const float up = gld(fld + (size_t)i * N + ((j + 1) & M)), down = gld(fld + (size_t)i * N + ((j - 1) & M));
+  const float vx = gld(ux + g), vy = gld(uy + g);
   if (SCHEME == NSGB_SCHEME_CENTRAL) {
     const float gx = divc(fsub(right, left), c.h2, c.rh2);
     const float gy = divc(fsub(up, down), c.h2, c.rh2);
-    out[g] = -fadd(fmul(vx, gx), fmul(vy, gy));
+    gst(out + g, -fadd(fmul(vx, gx), fmul(vy, gy)));
   } else {
     const float dfx = divc(vx >= 0.0f ? fsub(f, left) : fsub(right, f), c.h1, c.rh1);
     const float dfy = divc(vy >= 0.0f ? fsub(f, down) : fsub(up, f), c.h1, c.rh1);
-    out[g] = -fadd(fmul(vx, dfx), fmul(vy, dfy));
+    gst(out + g, -fadd(fmul(vx, dfx), fmul(vy, dfy)));
   }
 }
 
@@ -840,9 +839,9 @@ __global__ void k_forcing_field(const float* __restrict__ theta, float t, float*
   if (g >= NN) return;
   int i, j;
   ij_of(g, c, i, j);
-  const ForcingRow fr = forcing_time(__ldg(theta), __ldg(theta + 1), t, c);
-  f[g] = forcing_fx(i, fr, c);
-  f[NN + g] = 0.0f;
+  const ForcingRow fr = forcing_time(gldg(theta), gldg(theta + 1), t, c);
+  gst(f + g, forcing_fx(i, fr, c));
+  gst(f + NN + g, 0.0f);
 }
 
 static unsigned nb(const StepConsts& c) { return (unsigned)(((size_t)c.N * c.N + 255) / 256); }
@@ -873,5 +872,7 @@ cudaError_t launch_forcing_field(const float* theta, int theta_len, float t, flo
   k_forcing_field<<<nb(c), 256, 0, st>>>(theta, t, f, c);
   return cudaGetLastError();
 }
+
+NSGB_BOUNDS_UNIT(stencil, 1)
 
 }  // namespace nsgb
