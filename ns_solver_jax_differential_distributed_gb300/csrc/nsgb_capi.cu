@@ -1447,6 +1447,11 @@ int check_grad_members(const nsgb_grad_member* m, int count) {
     if (x.done_ops < 0 || x.done_ops > grad_ops_total(x.steps, x.every))
       return fail(NSGB_ERR_INVALID_ARG, "member %d: done_ops out of range", i);
   }
+  std::vector<const void*> states(count);
+  for (int i = 0; i < count; ++i) states[i] = m[i].state;
+  std::sort(states.begin(), states.end(), std::less<const void*>());
+  for (int i = 1; i < count; ++i)
+    if (states[i] == states[i - 1]) return fail(NSGB_ERR_INVALID_ARG, "two members share one state");
   return NSGB_OK;
 }
 

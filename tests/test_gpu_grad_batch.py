@@ -116,3 +116,17 @@ def test_refuses_capturing_stream(mods):
         finally:
             g.capture_end()
     assert rc == 1 and b"capturing" in lib.nsgb_last_error()
+
+
+def test_rejects_members_sharing_a_state(mods):
+    _native, ensemble = mods
+    N = 32
+    u0, th = _case(N, 0)
+    gb = ensemble.GradientBatch()
+    sid = gb.add(u0, th, 3, 2, L, 1e-3, 0.4 / N, "central")
+    m = gb._solves[sid]["member"]
+    lib = _native.lib()
+    arr = (_native.GradMember * 2)(m, m)
+    ws = torch.empty(lib.nsgb_grad_batch_workspace_bytes(2, 4), dtype=torch.uint8, device="cuda")
+    rc = lib.nsgb_grad_batch_advance(arr, 2, 4, ws.data_ptr(), ws.numel(), _native.stream_of(torch.device("cuda")))
+    assert rc == 1 and b"share" in lib.nsgb_last_error()
