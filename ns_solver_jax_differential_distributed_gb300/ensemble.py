@@ -196,7 +196,8 @@ class GradientBatch:
         self._ws = None
 
     def add(self, u0, theta, steps: int, every: int, L: float, nu: float, dt: float, scheme,
-            mu0: float = 0.5, sigma0: float = 0.1, C: float = 1.0, want_du0: bool = False) -> int:
+            mu0: float = 0.5, sigma0: float = 0.1, C: float = 1.0, want_du0: bool = False,
+            want_u_final: bool = False) -> int:
         u0 = _native._cuda_f32(torch.as_tensor(u0, dtype=torch.float32).to(self.device), "u0")
         theta = _native._cuda_f32(torch.as_tensor(theta, dtype=torch.float32).to(self.device), "theta")
         N = _native._square(u0, "u0", 2)
@@ -213,6 +214,7 @@ class GradientBatch:
             "J": torch.empty((), dtype=torch.float32, device=self.device),
             "g": torch.empty(theta.numel(), dtype=torch.float32, device=self.device),
             "du0": torch.empty_like(u0) if want_du0 else None,
+            "u_final": torch.empty_like(u0) if want_u_final else None,
             "total": int(lib.nsgb_grad_ops(steps, every)), "member": m,
         }
         m.u0 = u0.data_ptr()
@@ -220,7 +222,7 @@ class GradientBatch:
         m.theta_len = theta.numel()
         m.steps, m.every = steps, every
         m.J = rec["J"].data_ptr()
-        m.u_final = None
+        m.u_final = rec["u_final"].data_ptr() if want_u_final else None
         m.dJdtheta = rec["g"].data_ptr()
         m.dJdu0 = rec["du0"].data_ptr() if want_du0 else None
         m.state = state.data_ptr()
@@ -262,6 +264,10 @@ class GradientBatch:
 
     def du0(self, sid: int):
         return self._solves[sid]["du0"]
+
+    def u_final(self, sid: int):
+        """The final state (written when the forward phase ends)."""
+        return self._solves[sid]["u_final"]
 
     def release(self, sid: int):
         """Frees a finished (or abandoned) solve's device state."""

@@ -130,3 +130,24 @@ def test_rejects_members_sharing_a_state(mods):
     ws = torch.empty(lib.nsgb_grad_batch_workspace_bytes(2, 4), dtype=torch.uint8, device="cuda")
     rc = lib.nsgb_grad_batch_advance(arr, 2, 4, ws.data_ptr(), ws.numel(), _native.stream_of(torch.device("cuda")))
     assert rc == 1 and b"share" in lib.nsgb_last_error()
+
+
+def test_u_final_and_two_parameter_theta(mods):
+    """The final state written at the end of the forward phase, and theta
+    [A, B] (nu from the physics), against nsgb_rollout_grad."""
+    _native, ensemble = mods
+    gb = ensemble.GradientBatch()
+    ids, refs = [], []
+    for k, (N, scheme, steps, every) in enumerate([(64, "upwind", 11, 3), (128, "central", 4, 4)]):
+        u0, th = _case(N, k)
+        th2 = th[:2].contiguous()
+        J, g, uf, _ = _native.rollout_grad_raw(u0, th2, steps, every, L, 1e-3, 0.4 / N, scheme, want_u_final=True,
+                                               own_workspace=True)
+        refs.append((J.clone(), g.clone(), uf.clone()))
+        ids.append(gb.add(u0, th2, steps, every, L, 1e-3, 0.4 / N, scheme, want_u_final=True))
+    gb.run(5)
+    torch.cuda.synchronize()
+    for sid, (J, g, uf) in zip(ids, refs):
+        Jb, gb_ = gb.result(sid)
+        assert gb_.numel() == 2
+        assert torch.equal(Jb, J) and torch.equal(gb_, g) and torch.equal(gb.u_final(sid), uf)
