@@ -15,6 +15,13 @@ It launches few kernels, so it is the command to capture under ncu.
 times the backward steps of a 6-step gradient (adjoint stencil and FFT passes
 per step, every state stored) instead; ``--fused -1`` times the two kernels of
 the fused-row step (nsgb_plan_set_fused) instead of the four.
+
+    python -m ns_solver_jax_differential_distributed_gb300.profile_stages --N 128 --grad-batch 4
+
+runs COUNT gradient solves of N (12 steps, checkpoints every 4, seeded u0 and
+theta per solve) as one gradient batch (nsgb_grad_batch_advance) after a
+warm-up batch, and prints the batch's device time beside the solves run one
+after another: the command whose launch list shows the batched kernels.
 """
 from __future__ import annotations
 
@@ -147,6 +154,8 @@ def main(argv=None):
     ap.add_argument("--adjoint-tiles", default="", help="tw,th of the adjoint stencil")
     ap.add_argument("--tuned", action="store_true",
                     help="apply the autotuner's cached shapes for (N, scheme) first (as bench.py runs them)")
+    ap.add_argument("--grad-batch", type=int, default=0, metavar="COUNT",
+                    help="instead: COUNT gradient solves of N as one batch, against one after another")
     ap.add_argument("--fused", type=int, default=0, metavar="ROWS",
                     help="time the two-kernel step with the fused row kernel (bands of ROWS rows; -1: the "
                          "band that fits every cluster at once)")
@@ -168,6 +177,38 @@ def main(argv=None):
     if args.adjoint_tiles:
         plan.set_adjoint_tiles(*[int(x) for x in args.adjoint_tiles.split(",")])
     plan.set_fused(args.fused)
+    if args.grad_batch:
+        from .ensemble import GradientBatch
+        steps, every, nu = 12, 4, 1e-3
+        dt = 0.4 / args.N
+        cases = [(torch.from_numpy(spectral_u0(args.N, min(32, args.N // 4), k)).to(dev),
+                  torch.from_numpy(theta_draw(nu, k)).to(dev)) for k in range(args.grad_batch)]
+
+        def batched():
+            gb = GradientBatch(dev)
+            ids = [gb.add(u, t, steps, every, L, nu, dt, args.scheme) for u, t in cases]
+            gb.run(64)
+            return [gb.result(k)[1] for k in ids]
+
+        def sequential():
+            return [_native.rollout_grad_raw(u, t, steps, every, L, nu, dt, args.scheme, want_u_final=False,
+                                             own_workspace=True)[1] for u, t in cases]
+
+        res = {}
+        for name, fn in (("batched", batched), ("sequential", sequential)):
+            fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            g = fn()
+            e1.record()
+            torch.cuda.synchronize()
+            res[name] = (e0.elapsed_time(e1), g)
+        same = all(torch.equal(a, b) for a, b in zip(res["batched"][1], res["sequential"][1]))
+        print(json.dumps({"N": args.N, "scheme": args.scheme, "solves": args.grad_batch, "steps": steps,
+                          "every": every, "batched_ms": round(res["batched"][0], 4),
+                          "sequential_ms": round(res["sequential"][0], 4), "bitwise_equal": same}))
+        return
     if args.adjoint:
         # forward once, then `reps` backward phases (adjoint stencil + FFT
         # passes per step), timed with CUDA events; few launches, so the
