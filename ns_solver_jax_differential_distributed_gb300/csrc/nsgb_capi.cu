@@ -424,6 +424,71 @@ std::vector<EnsGraph> g_ens_graphs;
 cudaStream_t g_ens_streams[9] = {nullptr};
 cudaEvent_t g_ens_events[10] = {nullptr};
 
+// Eager fork/join of independent groups of batched launches: the groups'
+// kernels go to branch streams that start after the caller's stream's work so
+// far and that the caller's stream waits for at the join, so groups of
+// different N overlap on the device.  One pool per device; the lock is held
+// while a call enqueues (the events are reused).
+class Branches {
+ public:
+  static constexpr int kMax = 8;
+  // Forks n (1..kMax) branches off st; with n == 1 everything stays on st.
+  int open(cudaStream_t st, int n) {
+    st_ = st;
+    n_ = std::max(1, std::min(n, kMax));
+    if (n_ == 1) return NSGB_OK;
+    int dev = 0;
+    NSGB_CUDA(cudaGetDevice(&dev));
+    lk_ = std::unique_lock<std::mutex>(mu());
+    Pool& p = pools()[dev];
+    if (!p.ready) {
+      for (auto& x : p.s) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      NSGB_CUDA(cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming));
+      for (auto& x : p.join) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+      p.ready = true;
+    }
+    pool_ = &p;
+    NSGB_CUDA(cudaEventRecord(p.fork, st));
+    for (int b = 0; b < n_; ++b) NSGB_CUDA(cudaStreamWaitEvent(p.s[b], p.fork, 0));
+    return NSGB_OK;
+  }
+  cudaStream_t stream(int group) const { return n_ == 1 ? st_ : pool_->s[group % n_]; }
+  std::vector<cudaStream_t> streams() const {
+    std::vector<cudaStream_t> v;
+    for (int b = 0; b < n_; ++b) v.push_back(stream(b));
+    return v;
+  }
+  int close() {
+    if (n_ == 1) return NSGB_OK;
+    for (int b = 0; b < n_; ++b) {
+      NSGB_CUDA(cudaEventRecord(pool_->join[b], pool_->s[b]));
+      NSGB_CUDA(cudaStreamWaitEvent(st_, pool_->join[b], 0));
+    }
+    n_ = 1;
+    lk_ = std::unique_lock<std::mutex>();
+    return NSGB_OK;
+  }
+
+ private:
+  struct Pool {
+    bool ready = false;
+    cudaStream_t s[kMax] = {};
+    cudaEvent_t fork = nullptr, join[kMax] = {};
+  };
+  static std::mutex& mu() {
+    static std::mutex m;
+    return m;
+  }
+  static std::map<int, Pool>& pools() {
+    static std::map<int, Pool> p;
+    return p;
+  }
+  cudaStream_t st_ = nullptr;
+  int n_ = 1;
+  Pool* pool_ = nullptr;
+  std::unique_lock<std::mutex> lk_;
+};
+
 uint64_t fnv(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
   const unsigned char* c = (const unsigned char*)p;
   for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
@@ -1458,6 +1523,7 @@ int check_grad_members(const nsgb_grad_member* m, int count) {
 // Work of one tick, enqueued after the tick's tables are on the device.
 struct GradAction {
   enum Kind { GACC_ZERO, FWD, ADJ, GREDUCE, FFT, FWD_DONE, ADJ_DONE } kind;
+  int group;           // plan group (its branch stream)
   int member;          // GACC_ZERO, GREDUCE, FWD_DONE, ADJ_DONE
   const nsgb_plan* plan;
   int scheme;
@@ -1596,14 +1662,17 @@ int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops,
   std::vector<unsigned char> buf;
   buf.reserve(nsgb_grad_batch_workspace_bytes(count, std::min(ops, maxtodo)));
   std::vector<GradAction> acts;
+  int ngroups = 0;
   for (int k = 0; k < maxtodo; ++k) {
-    for (int g0 = 0; g0 < count;) {
+    int gi = 0;  // plan group index: the same for a plan in every tick
+    for (int g0 = 0; g0 < count; ++gi) {
       const nsgb_plan* plan = members[order[g0]].plan;
       int g1 = g0;
       while (g1 < count && members[order[g1]].plan == plan) ++g1;
       std::vector<SolveDev> fwd[2], fft;
       std::vector<AdjointArgs> adj[2];
       std::vector<GradAction> mid, post;
+      const size_t first_act = acts.size();
       for (int q = g0; q < g1; ++q) {
         const int i = order[q];
         if (k >= todo[i]) continue;
@@ -1686,13 +1755,18 @@ int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops,
         acts.push_back(z);
       }
       acts.insert(acts.end(), post.begin(), post.end());
+      for (size_t a = first_act; a < acts.size(); ++a) acts[a].group = gi;
       g0 = g1;
     }
+    ngroups = gi;
   }
   if (buf.size() > ws_bytes) return fail(NSGB_ERR_WORKSPACE, "gradient batch tables exceed the workspace");
   char* dev = (char*)workspace;
   if (!buf.empty()) NSGB_CUDA(cudaMemcpyAsync(dev, buf.data(), buf.size(), cudaMemcpyHostToDevice, st));
+  Branches br;  // the plan groups run side by side
+  if (int r = br.open(st, ngroups)) return r;
   for (const GradAction& z : acts) {
+    cudaStream_t st = br.stream(z.group);
     switch (z.kind) {
       case GradAction::GACC_ZERO:
         NSGB_CUDA(cudaMemsetAsync(ctx[z.member].g.gacc, 0, 4 * sizeof(double), st));
@@ -1730,6 +1804,7 @@ int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops,
       }
     }
   }
+  if (int r = br.close()) return r;
   return finish_call(st);
 }
 
@@ -1858,8 +1933,11 @@ int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void
   for (const EnsGroup& G : groups) maxtodo = std::max(maxtodo, G.todo);
   NSGB_CUDA(cudaMemcpyAsync(dev, tab.data(), sizeof(SolveDev) * count, cudaMemcpyHostToDevice, st));
   NSGB_CUDA(launch_counter_batch(dev, count, 0, false, st));  // counters = done_steps
-  std::vector<cudaStream_t> one{st};
-  for (int k = 0; k < maxtodo; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
+  Branches br;  // the groups run side by side
+  if (int r = br.open(st, (int)groups.size())) return r;
+  const std::vector<cudaStream_t> gs = br.streams();
+  for (int k = 0; k < maxtodo; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, gs));
+  if (int r = br.close()) return r;
   NSGB_CUDA(ensemble_finalize(members, order, tab, steps, (SolveDev*)(base + L.fin_off), st));
   return finish_call(st);
 }
