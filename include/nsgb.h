@@ -250,7 +250,9 @@ size_t nsgb_grad_batch_workspace_bytes(int count, int ops);
  * schedule, the members in lock-step.  At each step, the stencils of the
  * forward and recomputed steps of all members with the same plan and scheme
  * are ONE batched launch, their adjoint stencils another, and all their
- * FFT-Poisson solves one batched launch per pass.  Each member's J, u_final,
+ * FFT-Poisson solves one batched launch per pass; groups of different plans
+ * run side by side on internal streams joined back into `stream`.  Each
+ * member's J, u_final,
  * dJdtheta and dJdu0 equal those of nsgb_rollout_grad with the same
  * arguments bit for bit, however its work is split into calls and whatever
  * else is in the batch.  The caller advances done_ops itself.  Uploads its
@@ -283,9 +285,11 @@ size_t nsgb_ensemble_workspace_bytes(const nsgb_member* members, int count);
  * - done_steps) further steps from its saved state; members that reach
  * total_steps get u_final and J written.  Members with the same plan, scheme,
  * progress parity and step count form a group, and each stage of a step is
- * ONE batched launch per group (the member index is a grid dimension).  The
- * results equal one nsgb_rollout per member bit for bit.  The caller advances
- * done_steps itself. */
+ * ONE batched launch per group (the member index is a grid dimension); the
+ * groups run side by side on internal streams that start after the work
+ * already on `stream` and that `stream` waits for.  The results equal one
+ * nsgb_rollout per member bit for bit.  The caller advances done_steps
+ * itself. */
 int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void* workspace,
                           size_t workspace_bytes, void* stream);
 
