@@ -46,8 +46,11 @@ def _load() -> dict:
 
 
 def _store(data: dict) -> None:
+    # Several processes (one per GPU under torchrun) may tune at once: each
+    # writes its own temporary file and renames it over the cache, so every
+    # version of the cache on disk is complete (the last writer's entries win).
     os.makedirs(os.path.dirname(_CACHE_PATH), exist_ok=True)
-    tmp = _CACHE_PATH + ".tmp"
+    tmp = f"{_CACHE_PATH}.{os.getpid()}.tmp"
     with open(tmp, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
     os.replace(tmp, _CACHE_PATH)

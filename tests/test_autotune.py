@@ -3,6 +3,7 @@
 results (stencil bits; FFT radix to rounding)."""
 import json
 import math
+import os
 
 import pytest
 
@@ -68,3 +69,19 @@ def test_tune_applies_and_caches(cuda_lib, tmp_path, monkeypatch):
         plan.set_fft_radix(*old[1])
         plan.set_tiles(*old[0])
         plan.set_adjoint_tiles(*old[2])
+
+
+def test_cache_writes_from_concurrent_processes(tmp_path):
+    """Processes that store the tuning cache at the same time (one per GPU
+    under torchrun) each leave a complete file; none fails."""
+    import subprocess
+    import sys
+    path = tmp_path / "tiles.json"
+    code = ("import os, sys; os.environ['NSGB_TUNE_CACHE'] = sys.argv[1]\n"
+            "from ns_solver_jax_differential_distributed_gb300 import autotune\n"
+            "for i in range(200): autotune._store({'k%d' % i: [i] * 50})\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    procs = [subprocess.Popen([sys.executable, "-c", code, str(path)], cwd=root) for _ in range(4)]
+    assert all(p.wait(timeout=120) == 0 for p in procs)
+    assert len(json.load(open(path))) == 1
+    assert not [f for f in os.listdir(tmp_path) if f.endswith(".tmp")]
