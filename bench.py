@@ -361,7 +361,9 @@ def run_ours(args, world, rank, local):
                     "cold_frac": round(alg / (st_cold[dom] * 1e-3) / 1e9 / peak, 4),
                     "step_bytes_per_cell": sum(bytes_cell.values()),
                     "step_frac_of_32B_ideal": round(32.0 * value / world / (peak * 1e9), 4)}
-        cpu = None if args.no_cpu_baseline else cpu_baseline(w)
+        # the CPU baseline is timed at N=1 only: under torchrun the other
+        # ranks would hold their GPUs at the final barrier meanwhile
+        cpu = None if (args.no_cpu_baseline or world > 1) else cpu_baseline(w)
         result = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": warm, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
