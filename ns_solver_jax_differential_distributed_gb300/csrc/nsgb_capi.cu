@@ -468,6 +468,13 @@ class Branches {
     lk_ = std::unique_lock<std::mutex>();
     return NSGB_OK;
   }
+  // A call that returns early with an error still joins what it enqueued, so
+  // later work on the caller's stream never overtakes it.
+  ~Branches() {
+    if (n_ == 1) return;
+    for (int b = 0; b < n_; ++b)
+      if (cudaEventRecord(pool_->join[b], pool_->s[b]) == cudaSuccess) cudaStreamWaitEvent(st_, pool_->join[b], 0);
+  }
 
  private:
   struct Pool {
