@@ -210,7 +210,9 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
  * NSGB_ERR_BOUNDS with the first bad address, its size and the source line of
  * the access, instead of faulting.  In the normal build these calls do
  * nothing and return NSGB_OK; nsgb_bounds_checking() tells the builds apart
- * (1 when checking).  Registered ranges are [base, base + bytes). */
+ * (1 when checking).  Registered ranges are [base, base + bytes).  The
+ * checked build keeps one table of ranges per process and loads it into the
+ * current device whenever it changes: use it with one device. */
 int nsgb_bounds_checking(void);
 int nsgb_bounds_register(const void* base, size_t bytes);
 int nsgb_bounds_unregister(const void* base);
