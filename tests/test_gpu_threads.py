@@ -77,3 +77,42 @@ def test_concurrent_threads_match_sequential(nat, rows_plans):
     for t in threads:
         t.join()
     assert not errors, errors[:5]
+
+
+def test_concurrent_gradient_batches(nat):
+    """Gradient batches advanced from two host threads at once (each on its
+    own stream; their size groups fork onto the library's branch streams,
+    whose pool is shared) give the bits of the same batches run alone."""
+    from ns_solver_jax_differential_distributed_gb300 import ensemble
+
+    def batch(seed):
+        gb = ensemble.GradientBatch()
+        ids = []
+        for k, N in enumerate((64, 128, 64, 256)):
+            u0 = torch.from_numpy(spectral_u0(N, 8, seed + k)).cuda()
+            th = torch.tensor([0.9, 0.4, 2e-3], dtype=torch.float32, device="cuda")
+            ids.append(gb.add(u0, th, 10, 3, L, NU, 0.4 / N, "upwind"))
+        gb.run(7)
+        torch.cuda.current_stream().synchronize()
+        return [tuple(t.cpu() for t in gb.result(i)) for i in ids]
+
+    alone = {seed: batch(seed) for seed in (0, 100)}
+    errors = []
+
+    def worker(seed):
+        try:
+            with torch.cuda.stream(torch.cuda.Stream()):
+                for _ in range(3):
+                    got = batch(seed)
+                    for a, b in zip(got, alone[seed]):
+                        if not (torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])):
+                            errors.append((seed, a, b))
+        except Exception as exc:
+            errors.append((seed, repr(exc)))
+
+    threads = [threading.Thread(target=worker, args=(s,)) for s in (0, 100)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:3]
