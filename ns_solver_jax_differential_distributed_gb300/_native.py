@@ -105,6 +105,8 @@ SIGNATURES = {
     "nsgb_ensemble_workspace_bytes": ([ctypes.POINTER(Member), _I], _S),
     "nsgb_ensemble_advance": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
     "nsgb_ensemble_rollout": ([ctypes.POINTER(Member), _I, _I, _P, _S, _P], _I),
+    "nsgb_ensemble_persistent_workspace_bytes": ([ctypes.POINTER(Member), _I], _S),
+    "nsgb_ensemble_persistent": ([ctypes.POINTER(Member), _I, _P, _S, _P], _I),
     "nsgb_poisson_noalloc": ([_I, _D, _P, _P, _P], _I),
     "nsgb_bounds_checking": ([], _I),
     "nsgb_bounds_register": ([_P, _S], _I),

@@ -549,8 +549,10 @@ std::vector<EnsGroup> make_groups(const nsgb_member* m, int count, int steps, st
 }
 
 // Final projection and objective of the members that finish in this call.
+// tile_w/tile_h > 0: the objective partials follow that tiling instead of the
+// plans' stencil shapes (the persistent launch).
 cudaError_t ensemble_finalize(const nsgb_member* m, const std::vector<int>& order, const std::vector<SolveDev>& tab,
-                              int steps, SolveDev* fin_dev, cudaStream_t st) {
+                              int steps, SolveDev* fin_dev, cudaStream_t st, int tile_w = 0, int tile_h = 0) {
   std::vector<int> fin;
   for (size_t k = 0; k < order.size(); ++k) {
     const nsgb_member& x = m[order[k]];
@@ -582,7 +584,9 @@ cudaError_t ensemble_finalize(const nsgb_member* m, const std::vector<int>& orde
     const int n = (int)(b - a);
     e = launch_project_batch(fin_dev + a, n, variant_of(x.total_steps), x.plan->N, st);
     if (e == cudaSuccess)
-      e = launch_jreduce_batch(fin_dev + a, n, stencil_nblocks(x.plan->N, x.plan->tile_w, x.plan->tile_h),
+      e = launch_jreduce_batch(fin_dev + a, n,
+                               tile_w > 0 ? stencil_nblocks(x.plan->N, tile_w, tile_h)
+                                          : stencil_nblocks(x.plan->N, x.plan->tile_w, x.plan->tile_h),
                                x.total_steps, st);
     if (e != cudaSuccess) return e;
     a = b;
@@ -669,6 +673,7 @@ cudaError_t bounds_upload_fft(const bounds::Table& t);
 cudaError_t bounds_upload_adjoint(const bounds::Table& t);
 cudaError_t bounds_upload_fused(const bounds::Table& t);
 cudaError_t bounds_upload_optim(const bounds::Table& t);
+cudaError_t bounds_upload_persistent(const bounds::Table& t);
 }  // namespace nsgb
 namespace {
 std::mutex g_bounds_mu;
@@ -694,7 +699,7 @@ int bounds_upload_locked() {
     }
   t.report = g_bounds_report;
   for (auto up : {bounds_upload_stencil, bounds_upload_fft, bounds_upload_adjoint, bounds_upload_fused,
-                  bounds_upload_optim})
+                  bounds_upload_optim, bounds_upload_persistent})
     if ((e = up(t)) != cudaSuccess) return cuda_fail(e, "bounds table upload");
   return NSGB_OK;
 }
@@ -2039,6 +2044,119 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
   }
   for (int k = 0; k < steps - s; ++k) NSGB_CUDA(ensemble_step(groups, dev, k, one));
   NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + L.fin_off), st));
+  return finish_call(st);
+}
+
+}  // extern "C"
+
+namespace {
+// Workspace of nsgb_ensemble_persistent: the ensemble layout, then the member
+// constants, the stage item tables, the barrier words and, per member, the
+// objective partials of the 32 x 8 tiling.
+struct PersLayout {
+  EnsLayout ens;
+  size_t pm_off = 0, first_off = 0, bar_off = 0, bytes = 0;
+  std::vector<size_t> jpart_off;
+};
+
+constexpr int kPersTW = 32, kPersTH = 8;
+
+PersLayout pers_layout(const nsgb_member* m, int count) {
+  PersLayout P;
+  P.ens = ensemble_layout(m, count);
+  size_t off = P.ens.bytes;
+  P.pm_off = off;
+  off += align_up(sizeof(PersMember) * (size_t)count);
+  P.first_off = off;
+  off += align_up(sizeof(int) * 4 * (size_t)(count + 1));
+  P.bar_off = off;
+  off += align_up(4 * sizeof(unsigned));
+  P.jpart_off.resize(count);
+  for (int k = 0; k < count; ++k) {
+    P.jpart_off[k] = off;
+    off += align_up(sizeof(float) * (size_t)m[k].total_steps * stencil_nblocks(m[k].plan->N, kPersTW, kPersTH));
+  }
+  P.bytes = off;
+  return P;
+}
+}  // namespace
+
+extern "C" {
+
+size_t nsgb_ensemble_persistent_workspace_bytes(const nsgb_member* members, int count) {
+  if (!members || count <= 0) return 0;
+  for (int i = 0; i < count; ++i)
+    if (!members[i].plan || members[i].total_steps < 1 || !pers_supported(members[i].plan->N)) return 0;
+  return pers_layout(members, count).bytes;
+}
+
+int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* workspace, size_t ws_bytes,
+                             void* stream) {
+  if (int r = check_members(members_in, count, true)) return r;
+  const int steps = members_in[0].total_steps;
+  for (int i = 0; i < count; ++i) {
+    if (members_in[i].total_steps != steps)
+      return fail(NSGB_ERR_INVALID_ARG, "nsgb_ensemble_persistent needs equal total_steps");
+    if (!pers_supported(members_in[i].plan->N))
+      return fail(NSGB_ERR_UNSUPPORTED_N, "member %d: N=%d outside the persistent launch's 32..4096", i,
+                  members_in[i].plan->N);
+  }
+  std::vector<nsgb_member> members(members_in, members_in + count);
+  for (auto& m : members) m.done_steps = 0;
+  const PersLayout P = pers_layout(members.data(), count);
+  if (int r = check_ws(workspace, ws_bytes, P.bytes)) return r;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* base = (char*)workspace;
+  SolveDev* dev = (SolveDev*)(base + P.ens.tab_off);
+  std::vector<int> order;
+  (void)make_groups(members.data(), count, steps, order);
+  std::vector<SolveDev> tab(count);
+  std::vector<PersMember> pm(count);
+  std::vector<int> first(4 * (size_t)(count + 1), 0);
+  size_t smem = 0;
+  for (int k = 0; k < count; ++k) {
+    const int i = order[k];
+    const nsgb_member& x = members[i];
+    void* state = x.state ? x.state : (void*)(base + P.ens.state_off[i]);
+    tab[k] = make_solvedev(x, state);
+    float* jp = (float*)(base + P.jpart_off[i]);
+    for (auto& a : tab[k].st) {
+      a.jpart = jp;
+      a.jpart_rows = steps;
+    }
+    const int N = x.plan->N;
+    pm[k] = {x.plan->tw, x.plan->k2, (float)(1.0 / (2.0 * (double)N * (double)N)), N};
+    int it[4];
+    pers_items(N, it);
+    for (int s = 0; s < 4; ++s) first[(size_t)s * (count + 1) + k + 1] = first[(size_t)s * (count + 1) + k] + it[s];
+    smem = std::max(smem, pers_smem_bytes(N));
+  }
+  NSGB_CUDA(cudaMemcpyAsync(dev, tab.data(), sizeof(SolveDev) * count, cudaMemcpyHostToDevice, st));
+  NSGB_CUDA(cudaMemcpyAsync(base + P.pm_off, pm.data(), sizeof(PersMember) * count, cudaMemcpyHostToDevice, st));
+  NSGB_CUDA(cudaMemcpyAsync(base + P.first_off, first.data(), sizeof(int) * first.size(), cudaMemcpyHostToDevice,
+                            st));
+  unsigned* bar = (unsigned*)(base + P.bar_off);
+  NSGB_CUDA(cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned), st));
+  NSGB_CUDA(launch_counter_batch(dev, count, 0, false, st));  // step counters = 0
+  PersWork w;
+  w.dev = dev;
+  w.pm = (const PersMember*)(base + P.pm_off);
+  for (int s = 0; s < 4; ++s) {
+    w.first[s] = (const int*)(base + P.first_off) + (size_t)s * (count + 1);
+    w.items[s] = first[(size_t)s * (count + 1) + count];
+  }
+  w.count = count;
+  w.steps = steps;
+  w.done = 0;
+  w.bar = bar;
+  w.poll_limit = 1u << 22;
+  int dev_id = 0, sms = 152;
+  NSGB_CUDA(cudaGetDevice(&dev_id));
+  NSGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
+  NSGB_CUDA(launch_ensemble_persistent(w, smem, sms, nullptr, st));
+  NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + P.ens.fin_off), st, kPersTW,
+                              kPersTH));
+  NSGB_CUDA(launch_ensemble_poison(bar, dev, count, st));
   return finish_call(st);
 }
 

@@ -88,6 +88,32 @@ template <class T>
 __device__ __forceinline__ void gstcs(T* p, T v, int line = __builtin_LINE()) {
   if (bounds_ok(p, sizeof(T), line)) __stcs(p, v);
 }
+// L2-only load (__ldcg): for data other CTAs of the same launch wrote before
+// a grid-wide barrier (the non-coherent and L1 paths may hold stale lines).
+template <class T>
+__device__ __forceinline__ T gldcg(const T* p, int line = __builtin_LINE()) {
+  return bounds_ok(p, sizeof(T), line) ? __ldcg(p) : T{};
+}
+// Streamed load of a field: evict-first (__ldcs) in kernels whose inputs were
+// written by earlier launches, L2-only (__ldcg) in a persistent kernel
+// (COH) whose inputs other CTAs wrote during the launch.
+template <bool COH, class T>
+__device__ __forceinline__ T gldstream(const T* p, int line = __builtin_LINE()) {
+  if constexpr (COH) {
+    return gldcg(p, line);
+  } else {
+    return gldcs(p, line);
+  }
+}
+// Read-only-path load (__ldg) of a field, or L2-only in a persistent kernel.
+template <bool COH, class T>
+__device__ __forceinline__ T gldfield(const T* p, int line = __builtin_LINE()) {
+  if constexpr (COH) {
+    return gldcg(p, line);
+  } else {
+    return gldg(p, line);
+  }
+}
 // float4 views of float arrays (16-byte aligned offsets).
 __device__ __forceinline__ float4 gldg4(const float* p, int line = __builtin_LINE()) {
   return gldg(reinterpret_cast<const float4*>(p), line);

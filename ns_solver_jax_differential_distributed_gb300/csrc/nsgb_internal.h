@@ -108,6 +108,30 @@ cudaError_t launch_jreduce_batch(const SolveDev* solves, int count, int nblk, in
 cudaError_t launch_counter_batch(const SolveDev* solves, int count, int value, bool add, cudaStream_t st);
 cudaError_t poisson_fft_batch(int N, const FftLaunch& L, const SolveDev* solves, int count, cudaStream_t st);
 
+// ------------------------------------------------- persistent ensemble --
+// One cooperative launch for all steps of an ensemble (nsgb_ens_persistent.cu).
+struct PersMember {
+  const float2* tw;  // the member's plan twiddles (radix-16 tables first)
+  const float* k2;
+  float scale;       // 1 / (2 N^2)
+  int N;
+};
+struct PersWork {
+  const SolveDev* dev;     // members, in table order
+  const PersMember* pm;
+  const int* first[4];     // per stage (stencil, rows fwd, cols, rows inv): first item of each member, count + 1
+  int items[4];            // per stage: total items
+  int count, steps, done;  // members; steps of the launch; steps done before it
+  unsigned* bar;           // barrier words: arrivals, generation, abort (zeroed before the launch)
+  unsigned poll_limit;     // polls of a waiting CTA before it gives up
+};
+bool pers_supported(int N);        // N a power of two in [32, 4096]
+size_t pers_smem_bytes(int N);     // dynamic shared memory the items of N need
+void pers_items(int N, int out[4]);
+cudaError_t launch_ensemble_persistent(const PersWork& w, size_t smem, int sms, int* grid_out, cudaStream_t st);
+// J of every member non-finite when the launch gave up at a barrier
+cudaError_t launch_ensemble_poison(const unsigned* bar, const SolveDev* dev, int count, cudaStream_t st);
+
 // u_out = us - dt * grad(p)  (NS_solver.py:696-697)
 cudaError_t launch_project(const float* us, const float* p, float* u_out, const StepConsts& c,
                            cudaStream_t st);

@@ -141,6 +141,22 @@ class Ensemble:
             self.workspace.numel(), _native.stream_of(self.device)))
         return self.J, self.u_final
 
+    def run_persistent(self):
+        """The same ensemble in ONE persistent cooperative launch
+        (``nsgb_ensemble_persistent``): fields equal ``run()``'s with radix-16
+        transforms bit for bit; J to rounding (its partials follow a 32 x 8
+        tiling).  N a power of two in [32, 4096]."""
+        L = _bind()
+        need = L.nsgb_ensemble_persistent_workspace_bytes(self._members, len(self.specs))
+        if need == 0:
+            raise _native.NativeError("nsgb_ensemble_persistent_workspace_bytes", 1,
+                                      "members outside the persistent launch's sizes (32..4096)")
+        if getattr(self, "_pws", None) is None or self._pws.numel() < need:
+            self._pws = torch.empty(need, dtype=torch.uint8, device=self.device)
+        _native.check("nsgb_ensemble_persistent", L.nsgb_ensemble_persistent(
+            self._members, len(self.specs), self._pws.data_ptr(), self._pws.numel(), _native.stream_of(self.device)))
+        return self.J, self.u_final
+
     def run_advance(self, steps_per_call: int):
         """The same ensemble through nsgb_ensemble_advance in slices of
         ``steps_per_call`` steps (the continuous-batching entry point)."""

@@ -7,7 +7,8 @@ checks reads as well as writes on the kernels' real launch shapes: the
 single operators, both Poisson forms, solver steps, rollouts (tiled and
 row-streaming stencils, column bands with halo groups at N=4096, graph
 chunks, the fused row kernel), checkpointed gradients with the tiled and the
-row-streaming adjoint, an ensemble, a gradient batch and an optimiser loop.
+row-streaming adjoint, an ensemble (graph chunks and the persistent launch), a
+gradient batch and an optimiser loop.
 The checker itself is exercised by registering a buffer shorter than the
 kernel uses: the access beyond the registered end is reported (and skipped;
 the buffer itself is long enough, so nothing touches invalid memory)."""
@@ -187,6 +188,8 @@ def test_ensemble_and_gradient_batch(ctx):
         arr[k].state, arr[k].total_steps, arr[k].done_steps = None, 20, 0
     ws = ctx.ws(C.nsgb_ensemble_workspace_bytes(arr, len(sizes)))
     ctx.ok(C.nsgb_ensemble_rollout(arr, len(sizes), 8, ws.data_ptr(), ws.numel(), st))
+    pws = ctx.ws(C.nsgb_ensemble_persistent_workspace_bytes(arr, len(sizes)))
+    ctx.ok(C.nsgb_ensemble_persistent(arr, len(sizes), pws.data_ptr(), pws.numel(), st))
 
     cases = [(64, 9, 4, "upwind"), (128, 5, 2, "central"), (64, 3, 1, "central")]
     g_arr = (nat.GradMember * len(cases))()
