@@ -593,6 +593,10 @@ def run_optimize(args):
             "reference_cpu_s_per_gradient": 0.119, "dtype": "f32", "data": "synthetic"}
 
 
+def sizes_of(members):
+    return sorted({m.N for m in members})
+
+
 def run_ensemble(args):
     """Batching: 256 solves, N in {64,128,256,512} w.p. {.4,.3,.2,.1}, 500
     steps, per-solve nu/theta/u0; one batched launch per stage per N-group,
@@ -630,7 +634,18 @@ def run_ensemble(args):
     ens.tune_batched()
     clocks = ClockSampler(0).start()
     t_b, (Jb, ub) = timed(ens.run)
+    Jb, ub = Jb.clone(), [u.clone() for u in ub]
+    # the same ensemble in one persistent cooperative launch (stencil tiles
+    # 32 x 8, radix-16 transforms)
+    t_p, (Jp, up) = timed(ens.run_persistent)
     clock_info = clocks.stop()
+    radix16 = all(tuple(ensemble._native.get_plan(N, members[0].L, dev).fft_radix()) == (16, 16)
+                  for N in sizes_of(members))
+    pers = {"ms": t_p, "cell_steps_per_s": float(ens.cell_steps) / (t_p / 1e3),
+            "solves_per_s": len(members) / (t_p / 1e3), "vs_batched": t_b / t_p,
+            "fields_bitwise_equal_to_batched": all(torch.equal(a, b) for a, b in zip(up, ub)),
+            "plans_radix16": radix16,
+            "max_abs_field_diff": max(float((a - b).abs().max()) for a, b in zip(up, ub))}
     # fields are bit-identical across launch shapes; J sums per-block
     # partials, whose grouping follows the shape
     same = all(torch.equal(a, b) for a, b in zip(ub, us))
@@ -651,6 +666,7 @@ def run_ensemble(args):
                        "{.4,.3,.2,.1}", "steps": members[0].steps, "dt": members[0].dt,
                        "nu": "log-uniform [1e-4, 1e-2]", "theta": "within 20% of default, per solve",
                        "plain": "256 sequential single-solve rollouts (single-solve tuned shapes)"},
+            "persistent_launch": pers,
             "clocks": clock_info, "clocks_sequential": seq_clocks,
             "data": "synthetic", "chunk": 16}
 

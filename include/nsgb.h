@@ -305,12 +305,12 @@ int nsgb_ensemble_rollout(const nsgb_member* members, int count, int chunk, void
 
 /* The ensemble of nsgb_ensemble_rollout (members start from u0 and run equal
  * total_steps) advanced in ONE persistent cooperative launch: its CTAs walk a
- * work list per stage -- the 32 x 8 stencil tiles of every member, then the
+ * work list per stage -- the 64 x 16 stencil tiles of every member, then the
  * blocks of the forward row, column and inverse row transforms -- with a
  * bounded grid-wide barrier between stages, for every step.  Members' fields
  * equal their solo rollouts with radix-16 transforms bit for bit; the
- * objective partials follow the 32 x 8 tiling, so J agrees to rounding.  N a
- * power of two in [32, 4096] (NSGB_ERR_UNSUPPORTED_N otherwise).  If a CTA
+ * objective partials follow that tiling, so J agrees to rounding.  N a
+ * power of two in [64, 4096] (NSGB_ERR_UNSUPPORTED_N otherwise).  If a CTA
  * waits at a barrier beyond the launch's bound, the launch stops and every J
  * is NaN.  Workspace: nsgb_ensemble_persistent_workspace_bytes (0 on invalid
  * members). */

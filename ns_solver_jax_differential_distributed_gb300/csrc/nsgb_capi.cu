@@ -549,10 +549,10 @@ std::vector<EnsGroup> make_groups(const nsgb_member* m, int count, int steps, st
 }
 
 // Final projection and objective of the members that finish in this call.
-// tile_w/tile_h > 0: the objective partials follow that tiling instead of the
-// plans' stencil shapes (the persistent launch).
+// persistent: the objective partials follow the persistent launch's tiling
+// instead of the plans' stencil shapes.
 cudaError_t ensemble_finalize(const nsgb_member* m, const std::vector<int>& order, const std::vector<SolveDev>& tab,
-                              int steps, SolveDev* fin_dev, cudaStream_t st, int tile_w = 0, int tile_h = 0) {
+                              int steps, SolveDev* fin_dev, cudaStream_t st, bool persistent = false) {
   std::vector<int> fin;
   for (size_t k = 0; k < order.size(); ++k) {
     const nsgb_member& x = m[order[k]];
@@ -583,11 +583,9 @@ cudaError_t ensemble_finalize(const nsgb_member* m, const std::vector<int>& orde
     }
     const int n = (int)(b - a);
     e = launch_project_batch(fin_dev + a, n, variant_of(x.total_steps), x.plan->N, st);
-    if (e == cudaSuccess)
-      e = launch_jreduce_batch(fin_dev + a, n,
-                               tile_w > 0 ? stencil_nblocks(x.plan->N, tile_w, tile_h)
-                                          : stencil_nblocks(x.plan->N, x.plan->tile_w, x.plan->tile_h),
-                               x.total_steps, st);
+    int tw = x.plan->tile_w, th = x.plan->tile_h;
+    if (persistent) pers_tile(x.plan->N, tw, th);
+    if (e == cudaSuccess) e = launch_jreduce_batch(fin_dev + a, n, stencil_nblocks(x.plan->N, tw, th), x.total_steps, st);
     if (e != cudaSuccess) return e;
     a = b;
   }
@@ -2052,14 +2050,12 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
 namespace {
 // Workspace of nsgb_ensemble_persistent: the ensemble layout, then the member
 // constants, the stage item tables, the barrier words and, per member, the
-// objective partials of the 32 x 8 tiling.
+// objective partials of the persistent launch's tiling.
 struct PersLayout {
   EnsLayout ens;
   size_t pm_off = 0, first_off = 0, bar_off = 0, bytes = 0;
   std::vector<size_t> jpart_off;
 };
-
-constexpr int kPersTW = 32, kPersTH = 8;
 
 PersLayout pers_layout(const nsgb_member* m, int count) {
   PersLayout P;
@@ -2074,7 +2070,9 @@ PersLayout pers_layout(const nsgb_member* m, int count) {
   P.jpart_off.resize(count);
   for (int k = 0; k < count; ++k) {
     P.jpart_off[k] = off;
-    off += align_up(sizeof(float) * (size_t)m[k].total_steps * stencil_nblocks(m[k].plan->N, kPersTW, kPersTH));
+    int tw, th;
+    pers_tile(m[k].plan->N, tw, th);
+    off += align_up(sizeof(float) * (size_t)m[k].total_steps * stencil_nblocks(m[k].plan->N, tw, th));
   }
   P.bytes = off;
   return P;
@@ -2098,7 +2096,7 @@ int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* wor
     if (members_in[i].total_steps != steps)
       return fail(NSGB_ERR_INVALID_ARG, "nsgb_ensemble_persistent needs equal total_steps");
     if (!pers_supported(members_in[i].plan->N))
-      return fail(NSGB_ERR_UNSUPPORTED_N, "member %d: N=%d outside the persistent launch's 32..4096", i,
+      return fail(NSGB_ERR_UNSUPPORTED_N, "member %d: N=%d outside the persistent launch's 64..4096", i,
                   members_in[i].plan->N);
   }
   std::vector<nsgb_member> members(members_in, members_in + count);
@@ -2154,8 +2152,7 @@ int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* wor
   NSGB_CUDA(cudaGetDevice(&dev_id));
   NSGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev_id));
   NSGB_CUDA(launch_ensemble_persistent(w, smem, sms, nullptr, st));
-  NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + P.ens.fin_off), st, kPersTW,
-                              kPersTH));
+  NSGB_CUDA(ensemble_finalize(members.data(), order, tab, steps, (SolveDev*)(base + P.ens.fin_off), st, true));
   NSGB_CUDA(launch_ensemble_poison(bar, dev, count, st));
   return finish_call(st);
 }

@@ -3,9 +3,9 @@
 // stage -- the stencil tiles of all members, then their forward row-transform
 // blocks, column blocks and inverse row-transform blocks -- and meet at a
 // grid-wide barrier between stages.  Each work item runs the same body as the
-// stage's own kernel (tiled stencil 32 x 8, radix-16 transforms), so a member's
-// fields equal those of its solo rollout with radix-16 transforms bit for bit;
-// its objective partials follow the 32 x 8 tiling.
+// stage's own kernel (tiled stencil 64 x 16, radix-16 transforms), so a
+// member's fields equal those of its solo rollout with radix-16 transforms bit
+// for bit; its objective partials follow the 64 x 16 tiling.
 //
 // Loads of fields other CTAs wrote during the launch go through L2 only
 // (__ldcg): the non-coherent read-only path and L1 could return lines of an
@@ -19,7 +19,7 @@ namespace nsgb {
 namespace pers {
 
 constexpr int kThreads = 256;  // blockDim (32, 8): the tiled stencil's CTA
-constexpr int kTW = 32, kTH = 8;
+constexpr int kTW = 64, kTH = 16;  // stencil tile
 
 __host__ __device__ inline int fft_T(int N) { return N / 16; }
 // Row pairs of one forward/inverse row item, and spectrum rows of one column
@@ -81,7 +81,7 @@ __device__ __forceinline__ void rows_inv_item(const FftPtrs& f, const PersMember
   rows_inv_body<N, 16, true>(f.spec, f.p, pm.tw, tid % fft_T(N), tid / fft_T(N), rows_P(N), u);
 }
 
-#define NSGB_PERS_SIZES(X) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
+#define NSGB_PERS_SIZES(X) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096)
 
 // Bounded to 80 registers for three CTAs per SM (the union of the stage bodies
 // would otherwise take about 200 and leave one).
@@ -90,7 +90,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ensemble_persistent(const PersW
   for (int k = 0; k < w.steps; ++k) {
     const int s = w.done + k;
     const int variant = s == 0 ? 0 : ((s & 1) ? 1 : 2);
-    // 1. fused stencil of every member, tile by tile
+    // 1. fused stencil of every member, tile by tile (64 x 16 tiles)
     for (int it = blockIdx.x; it < w.items[0]; it += gridDim.x) {
       const int m = member_of(w.first[0], w.count, it);
       const int u = it - __ldg(w.first[0] + m);
@@ -139,6 +139,12 @@ __global__ void k_ensemble_poison(const unsigned* __restrict__ bar, const SolveD
 }  // namespace pers
 
 // Host side ------------------------------------------------------------------
+void pers_tile(int N, int& tw, int& th) {
+  (void)N;
+  tw = pers::kTW;
+  th = pers::kTH;
+}
+
 size_t pers_smem_bytes(int N) {
   const size_t stencil = sizeof(float) * StencilSmem<pers::kTW, pers::kTH>::FLOATS;
   const int T = pers::fft_T(N);
@@ -150,13 +156,15 @@ size_t pers_smem_bytes(int N) {
 
 void pers_items(int N, int out[4]) {
   const int T = pers::fft_T(N);
-  out[0] = (N / pers::kTW) * (N / pers::kTH);
+  int tw, th;
+  pers_tile(N, tw, th);
+  out[0] = (N / tw) * (N / th);
   out[1] = out[3] = N / (2 * pers::rows_P(N));
   const int KB = pers::kThreads / T;
   out[2] = (N / 2 + 1 + KB - 1) / KB;
 }
 
-bool pers_supported(int N) { return N >= 32 && N <= 4096 && (N & (N - 1)) == 0; }
+bool pers_supported(int N) { return N >= 64 && N <= 4096 && (N & (N - 1)) == 0; }
 
 cudaError_t launch_ensemble_persistent(const PersWork& w, size_t smem, int sms, int* grid_out, cudaStream_t st) {
   cudaError_t e = raise_smem_limit(pers::k_ensemble_persistent);

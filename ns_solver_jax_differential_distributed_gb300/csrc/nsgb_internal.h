@@ -125,7 +125,8 @@ struct PersWork {
   unsigned* bar;           // barrier words: arrivals, generation, abort (zeroed before the launch)
   unsigned poll_limit;     // polls of a waiting CTA before it gives up
 };
-bool pers_supported(int N);        // N a power of two in [32, 4096]
+bool pers_supported(int N);        // N a power of two in [64, 4096]
+void pers_tile(int N, int& tw, int& th);  // stencil tile of the persistent launch
 size_t pers_smem_bytes(int N);     // dynamic shared memory the items of N need
 void pers_items(int N, int out[4]);
 cudaError_t launch_ensemble_persistent(const PersWork& w, size_t smem, int sms, int* grid_out, cudaStream_t st);

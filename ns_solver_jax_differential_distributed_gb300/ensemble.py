@@ -144,13 +144,13 @@ class Ensemble:
     def run_persistent(self):
         """The same ensemble in ONE persistent cooperative launch
         (``nsgb_ensemble_persistent``): fields equal ``run()``'s with radix-16
-        transforms bit for bit; J to rounding (its partials follow a 32 x 8
-        tiling).  N a power of two in [32, 4096]."""
+        transforms bit for bit; J to rounding (its partials follow 64 x 16
+        tiles).  N a power of two in [64, 4096]."""
         L = _bind()
         need = L.nsgb_ensemble_persistent_workspace_bytes(self._members, len(self.specs))
         if need == 0:
             raise _native.NativeError("nsgb_ensemble_persistent_workspace_bytes", 1,
-                                      "members outside the persistent launch's sizes (32..4096)")
+                                      "members outside the persistent launch's sizes (64..4096)")
         if getattr(self, "_pws", None) is None or self._pws.numel() < need:
             self._pws = torch.empty(need, dtype=torch.uint8, device=self.device)
         _native.check("nsgb_ensemble_persistent", L.nsgb_ensemble_persistent(

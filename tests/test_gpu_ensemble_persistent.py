@@ -2,7 +2,7 @@
 launch advances every member of an uneven ensemble through all its steps.
 Fields equal the graph-chunked ensemble and the members' solo rollouts bit
 for bit (radix-16 transforms); J agrees to rounding (its partials follow the
-32 x 8 tiling); repeated launches give the same bits."""
+persistent launch's 64 x 16 tiling); repeated launches give the same bits."""
 import math
 
 import numpy as np
@@ -14,7 +14,7 @@ from ns_solver_jax_differential_distributed_gb300.workloads import spectral_u0
 pytestmark = pytest.mark.gpu
 
 L = 2 * math.pi
-SIZES = [32, 64, 128, 256, 512, 1024, 64, 128, 2048]
+SIZES = [64, 128, 256, 512, 1024, 64, 128, 2048, 4096]
 SCHEMES = ["central", "upwind", "upwind", "central", "upwind", "central", "central", "upwind", "upwind"]
 
 
@@ -70,7 +70,7 @@ def test_persistent_equals_chunked_and_solo(mods, radix16):
 
 def test_unsupported_size_rejected(mods):
     _native, ensemble = mods
-    N = 16
+    N = 32
     spec = ensemble.SolveSpec(N, spectral_u0(N, 4, 0), np.array([1.0, 0.5, 1e-3], np.float32), 1e-3, 1e-3,
                               "central", L)
     ens = ensemble.Ensemble([spec], steps=4, chunk=0)
