@@ -2108,6 +2108,9 @@ int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* wor
   SolveDev* dev = (SolveDev*)(base + P.ens.tab_off);
   std::vector<int> order;
   (void)make_groups(members.data(), count, steps, order);
+  // largest members first: their items lead every stage's work list, so the
+  // list ends with short items and the CTAs finish a stage close together
+  std::reverse(order.begin(), order.end());
   std::vector<SolveDev> tab(count);
   std::vector<PersMember> pm(count);
   std::vector<int> first(4 * (size_t)(count + 1), 0);
