@@ -122,7 +122,7 @@ class Ensemble:
                 except _native.NativeError:
                     continue
                 self._ensure_workspace()
-                ms = self._time_run()
+                ms = min(self._time_run() for _ in range(2))  # the better of two: less timing noise
                 if best_ms is None or ms < best_ms:
                     best, best_ms = (tw, th), ms
             plan.set_tiles(best[0], best[1], base[2], base[3])
