@@ -312,7 +312,8 @@ int nsgb_ensemble_rollout(const nsgb_member* members, int count, int chunk, void
  * objective partials follow that tiling, so J agrees to rounding.  N a
  * power of two in [64, 4096] (NSGB_ERR_UNSUPPORTED_N otherwise).  If a CTA
  * waits at a barrier beyond the launch's bound, the launch stops and every J
- * is NaN.  Workspace: nsgb_ensemble_persistent_workspace_bytes (0 on invalid
+ * is NaN.  Refuses a capturing stream (it uploads its tables from host
+ * memory).  Workspace: nsgb_ensemble_persistent_workspace_bytes (0 on invalid
  * members). */
 size_t nsgb_ensemble_persistent_workspace_bytes(const nsgb_member* members, int count);
 int nsgb_ensemble_persistent(const nsgb_member* members, int count, void* workspace, size_t workspace_bytes,

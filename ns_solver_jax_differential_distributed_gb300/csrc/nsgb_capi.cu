@@ -2104,6 +2104,11 @@ int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* wor
   const PersLayout P = pers_layout(members.data(), count);
   if (int r = check_ws(workspace, ws_bytes, P.bytes)) return r;
   cudaStream_t st = (cudaStream_t)stream;
+  // the call uploads its tables from host memory that does not outlive it
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  NSGB_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(NSGB_ERR_INVALID_ARG, "nsgb_ensemble_persistent does not run on a capturing stream");
   char* base = (char*)workspace;
   SolveDev* dev = (SolveDev*)(base + P.ens.tab_off);
   std::vector<int> order;
