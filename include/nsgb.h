@@ -291,7 +291,9 @@ size_t nsgb_ensemble_workspace_bytes(const nsgb_member* members, int count);
  * groups run side by side on internal streams that start after the work
  * already on `stream` and that `stream` waits for.  The results equal one
  * nsgb_rollout per member bit for bit.  The caller advances done_steps
- * itself. */
+ * itself.  It uploads the member table from host memory, so it refuses a
+ * capturing stream (as does nsgb_ensemble_rollout, which captures its step
+ * chunks itself). */
 int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void* workspace,
                           size_t workspace_bytes, void* stream);
 

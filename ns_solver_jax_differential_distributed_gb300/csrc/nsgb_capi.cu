@@ -316,6 +316,18 @@ int check_field(const float* f, const char* name) {
   return NSGB_OK;
 }
 
+// Calls that upload their argument tables from host memory that does not
+// outlive them refuse a capturing stream: a captured copy would read that
+// memory again at every replay.
+int refuse_capture(cudaStream_t st, const char* fn) {
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(NSGB_ERR_INVALID_ARG, "%s does not run on a capturing stream (it uploads tables from host memory)", fn);
+  return NSGB_OK;
+}
+
 int check_theta(const float* theta, int theta_len) {
   if (!theta) return fail(NSGB_ERR_INVALID_ARG, "theta is NULL");
   if (theta_len != 2 && theta_len != 3)
@@ -1648,11 +1660,7 @@ int nsgb_grad_batch_advance(const nsgb_grad_member* members, int count, int ops,
   if (ops == 0) return NSGB_OK;
   if (int r = check_ws(workspace, ws_bytes, nsgb_grad_batch_workspace_bytes(count, ops))) return r;
   cudaStream_t st = (cudaStream_t)stream;
-  // Each call uploads its argument tables from host memory.
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  NSGB_CUDA(cudaStreamIsCapturing(st, &cap));
-  if (cap != cudaStreamCaptureStatusNone)
-    return fail(NSGB_ERR_INVALID_ARG, "nsgb_grad_batch_advance does not run on a capturing stream");
+  if (int r = refuse_capture(st, "nsgb_grad_batch_advance")) return r;
 
   std::vector<GradMemberCtx> ctx;
   ctx.reserve(count);
@@ -1929,6 +1937,7 @@ int nsgb_ensemble_advance(const nsgb_member* members, int count, int steps, void
   EnsLayout L = ensemble_layout(members, count);
   if (int r = check_ws(workspace, ws_bytes, L.bytes)) return r;
   cudaStream_t st = (cudaStream_t)stream;
+  if (int r = refuse_capture(st, "nsgb_ensemble_advance")) return r;
   char* base = (char*)workspace;
   SolveDev* dev = (SolveDev*)(base + L.tab_off);
   std::vector<int> order;
@@ -1965,6 +1974,7 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
   EnsLayout L = ensemble_layout(members.data(), count);
   if (int r = check_ws(workspace, ws_bytes, L.bytes)) return r;
   cudaStream_t st = (cudaStream_t)stream;
+  if (int r = refuse_capture(st, "nsgb_ensemble_rollout")) return r;
   char* base = (char*)workspace;
   SolveDev* dev = (SolveDev*)(base + L.tab_off);
   std::vector<int> order;
@@ -2104,11 +2114,7 @@ int nsgb_ensemble_persistent(const nsgb_member* members_in, int count, void* wor
   const PersLayout P = pers_layout(members.data(), count);
   if (int r = check_ws(workspace, ws_bytes, P.bytes)) return r;
   cudaStream_t st = (cudaStream_t)stream;
-  // the call uploads its tables from host memory that does not outlive it
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  NSGB_CUDA(cudaStreamIsCapturing(st, &cap));
-  if (cap != cudaStreamCaptureStatusNone)
-    return fail(NSGB_ERR_INVALID_ARG, "nsgb_ensemble_persistent does not run on a capturing stream");
+  if (int r = refuse_capture(st, "nsgb_ensemble_persistent")) return r;
   char* base = (char*)workspace;
   SolveDev* dev = (SolveDev*)(base + P.ens.tab_off);
   std::vector<int> order;

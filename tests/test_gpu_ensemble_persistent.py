@@ -76,3 +76,30 @@ def test_unsupported_size_rejected(mods):
     ens = ensemble.Ensemble([spec], steps=4, chunk=0)
     with pytest.raises(_native.NativeError):
         ens.run_persistent()
+
+
+def test_table_uploading_calls_refuse_capture(mods):
+    """The ensemble calls upload their member tables from host memory that
+    does not outlive the call, so inside a stream capture they return
+    NSGB_ERR_INVALID_ARG and enqueue nothing."""
+    import ctypes
+    _native, ensemble = mods
+    N = 64
+    spec = ensemble.SolveSpec(N, spectral_u0(N, 8, 0), np.array([1.0, 0.5, 1e-3], np.float32), 1e-3, 1e-3,
+                              "central", L)
+    ens = ensemble.Ensemble([spec], steps=4, chunk=0)
+    lib = _native.lib()
+    need = lib.nsgb_ensemble_persistent_workspace_bytes(ens._members, 1)
+    pws = torch.empty(need, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        try:
+            st = ctypes.c_void_p(s.cuda_stream)
+            rcs = [lib.nsgb_ensemble_rollout(ens._members, 1, 0, ens.workspace.data_ptr(), ens.workspace.numel(), st),
+                   lib.nsgb_ensemble_advance(ens._members, 1, 2, ens.workspace.data_ptr(), ens.workspace.numel(), st),
+                   lib.nsgb_ensemble_persistent(ens._members, 1, pws.data_ptr(), pws.numel(), st)]
+        finally:
+            g.capture_end()
+    assert rcs == [1, 1, 1], rcs
