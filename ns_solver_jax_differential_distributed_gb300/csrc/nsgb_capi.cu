@@ -90,8 +90,7 @@ struct nsgb_plan {
   int adj_w = 64, adj_h = 16;  // tiled-kernel shape of the adjoint stencil
   int radix_rows = 16, radix_cols = 16;  // Stockham radix of the FFT passes
   int fused_rows = 0;  // row band of the fused row kernel (0: the four-kernel step)
-  cudaStream_t graph_stream = nullptr;
-  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  cudaStream_t graph_stream = nullptr;  // private stream graphs are captured on
   std::vector<GraphEntry> graphs;
   // gradient calls: the last call's arguments, and graphs of calls repeated
   // with identical arguments
@@ -909,8 +908,6 @@ int nsgb_plan_destroy(nsgb_plan* plan) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
   for (auto& g : plan->grad_graphs) cudaGraphExecDestroy(g.second);
   if (plan->graph_stream) cudaStreamDestroy(plan->graph_stream);
-  if (plan->ev_in) cudaEventDestroy(plan->ev_in);
-  if (plan->ev_out) cudaEventDestroy(plan->ev_out);
   bounds_remove_library_range(plan->tw);
   bounds_remove_library_range(plan->k2);
   cudaFree(plan->tw);
@@ -1196,11 +1193,7 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
         break;
       }
     }
-    if (!plan->graph_stream) {
-      NSGB_CUDA(cudaStreamCreateWithFlags(&plan->graph_stream, cudaStreamNonBlocking));
-      NSGB_CUDA(cudaEventCreateWithFlags(&plan->ev_in, cudaEventDisableTiming));
-      NSGB_CUDA(cudaEventCreateWithFlags(&plan->ev_out, cudaEventDisableTiming));
-    }
+    if (!plan->graph_stream) NSGB_CUDA(cudaStreamCreateWithFlags(&plan->graph_stream, cudaStreamNonBlocking));
     if (!ge) {
       if (plan->graphs.size() >= 8) {
         cudaGraphExecDestroy(plan->graphs.front().exec);
@@ -1246,15 +1239,13 @@ int nsgb_rollout(const nsgb_plan* plan_c, const nsgb_phys* phys, const float* u0
     }
     // The chunk graph reads its first step index from w.ctr and advances it
     // by K in its last node, so one instantiated graph serves every chunk.
-    NSGB_CUDA(cudaEventRecord(plan->ev_in, st));
-    NSGB_CUDA(cudaStreamWaitEvent(plan->graph_stream, plan->ev_in, 0));
-    NSGB_CUDA(launch_step_counter(w.ctr, s, false, plan->graph_stream));
+    // Graphs are captured on the plan's private stream and replayed on the
+    // caller's, so callers on different streams overlap on the device.
+    NSGB_CUDA(launch_step_counter(w.ctr, s, false, st));
     while (steps - s >= K) {
-      NSGB_CUDA(cudaGraphLaunch(ge->exec, plan->graph_stream));
+      NSGB_CUDA(cudaGraphLaunch(ge->exec, st));
       s += K;
     }
-    NSGB_CUDA(cudaEventRecord(plan->ev_out, plan->graph_stream));
-    NSGB_CUDA(cudaStreamWaitEvent(st, plan->ev_out, 0));
     cur = w.usA;
     spec_cur = w.spec;
   }
@@ -1430,11 +1421,7 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
                                  dJdu0, workspace, st);
       return r ? r : finish_call(st);
     }
-    if (!pl->graph_stream) {
-      NSGB_CUDA(cudaStreamCreateWithFlags(&pl->graph_stream, cudaStreamNonBlocking));
-      NSGB_CUDA(cudaEventCreateWithFlags(&pl->ev_in, cudaEventDisableTiming));
-      NSGB_CUDA(cudaEventCreateWithFlags(&pl->ev_out, cudaEventDisableTiming));
-    }
+    if (!pl->graph_stream) NSGB_CUDA(cudaStreamCreateWithFlags(&pl->graph_stream, cudaStreamNonBlocking));
     cudaGraph_t graph = nullptr;
     NSGB_CUDA(cudaStreamBeginCapture(pl->graph_stream, cudaStreamCaptureModeThreadLocal));
     const int r = grad_enqueue(plan, phys, u0, theta, theta_len, steps, every, phases, J, u_final, dJdtheta,
@@ -1454,11 +1441,8 @@ int nsgb_rollout_grad(const nsgb_plan* plan, const nsgb_phys* phys, const float*
     }
     pl->grad_graphs.emplace_back(key, exec);
   }
-  NSGB_CUDA(cudaEventRecord(pl->ev_in, st));
-  NSGB_CUDA(cudaStreamWaitEvent(pl->graph_stream, pl->ev_in, 0));
-  NSGB_CUDA(cudaGraphLaunch(exec, pl->graph_stream));
-  NSGB_CUDA(cudaEventRecord(pl->ev_out, pl->graph_stream));
-  NSGB_CUDA(cudaStreamWaitEvent(st, pl->ev_out, 0));
+  // captured on the plan's private stream, replayed on the caller's
+  NSGB_CUDA(cudaGraphLaunch(exec, st));
   return finish_call(st);
 }
 

@@ -106,13 +106,20 @@ class ParameterOptimizationStudy:
         logger.info(f"ParameterOptimizationStudy initialized: {len(self.optim_configs)} optimizers, "
                     f"{self.optim_steps} steps")
 
-    def _run_single_optimizer(self, name: str, optimizer: OptimizerSpec) -> dict:
+    def _launch_optimizer(self, optimizer: OptimizerSpec):
+        """Enqueue one optimiser's whole loop on the current stream; device
+        tensors (objectives, parameters)."""
         s = self.solver
         g, ph = s.grid, s.phys
-        objectives, parameters = _native.optimize(
+        return _native.optimize(
             self.theta0.to(s.device), int(s.time.steps), s._every(), g.N, float(g.L), float(ph.nu),
             float(s.time.dt), s._scheme_id, optimizer.native(), self.optim_steps, u0=None,
             mu0=float(ph.mu0), sigma0=float(ph.sigma0), C=float(ph.C))
+
+    def _run_single_optimizer(self, name: str, optimizer: OptimizerSpec) -> dict:
+        return self._collect(name, *self._launch_optimizer(optimizer))
+
+    def _collect(self, name: str, objectives, parameters) -> dict:
         objectives = objectives.cpu().numpy()
         parameters = parameters.cpu().numpy()
         obj_initial = float(objectives[0])
@@ -131,10 +138,42 @@ class ParameterOptimizationStudy:
         }
 
     def run_all(self) -> dict:
+        """Every optimiser's loop, each enqueued by its own host thread on its
+        own CUDA stream, so the loops overlap on the device (they share
+        nothing: each has its own workspace and graph; one thread alone
+        would wait for the launch queue it fills); results equal running them
+        one by one."""
+        import threading
         logger.info(f"Testing {len(self.optim_configs)} optimizer configurations over {self.optim_steps} steps")
+        dev = self.solver.device
+        cur = torch.cuda.current_stream(dev)
+        sides = [torch.cuda.Stream(dev) for _ in self.optim_configs]
+        outs = [None] * len(sides)
+        errors = []
+
+        def enqueue(k, cfg):
+            try:
+                torch.cuda.set_device(dev)
+                with torch.cuda.stream(sides[k]):
+                    outs[k] = self._launch_optimizer(cfg["optimizer"])
+            except Exception as exc:  # re-raised on the caller's thread
+                errors.append(exc)
+
+        for side in sides:
+            side.wait_stream(cur)
+        threads = [threading.Thread(target=enqueue, args=(k, cfg)) for k, cfg in enumerate(self.optim_configs)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if errors:
+            raise errors[0]
         results = {}
-        for cfg in self.optim_configs:
-            results[cfg["name"]] = self._run_single_optimizer(cfg["name"], cfg["optimizer"])
+        for cfg, side, out in zip(self.optim_configs, sides, outs):
+            cur.wait_stream(side)
+            for t in out:
+                t.record_stream(cur)
+            results[cfg["name"]] = self._collect(cfg["name"], *out)
         self.results = results
         return results
 
