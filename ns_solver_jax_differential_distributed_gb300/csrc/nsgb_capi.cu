@@ -444,22 +444,27 @@ class Branches {
  public:
   static constexpr int kMax = 8;
   // Forks n (1..kMax) branches off st; with n == 1 everything stays on st.
+  // The branch count is set only once the pool exists, so a failure while
+  // creating it leaves a one-branch object whose destructor joins nothing.
   int open(cudaStream_t st, int n) {
     st_ = st;
-    n_ = std::max(1, std::min(n, kMax));
-    if (n_ == 1) return NSGB_OK;
+    n = std::max(1, std::min(n, kMax));
+    if (n == 1) return NSGB_OK;
     int dev = 0;
     NSGB_CUDA(cudaGetDevice(&dev));
     lk_ = std::unique_lock<std::mutex>(mu());
     Pool& p = pools()[dev];
     if (!p.ready) {
-      for (auto& x : p.s) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
-      NSGB_CUDA(cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming));
-      for (auto& x : p.join) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+      for (auto& x : p.s)
+        if (!x) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      if (!p.fork) NSGB_CUDA(cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming));
+      for (auto& x : p.join)
+        if (!x) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
       p.ready = true;
     }
     pool_ = &p;
     NSGB_CUDA(cudaEventRecord(p.fork, st));
+    n_ = n;  // from here on the destructor joins every branch
     for (int b = 0; b < n_; ++b) NSGB_CUDA(cudaStreamWaitEvent(p.s[b], p.fork, 0));
     return NSGB_OK;
   }
@@ -482,7 +487,7 @@ class Branches {
   // A call that returns early with an error still joins what it enqueued, so
   // later work on the caller's stream never overtakes it.
   ~Branches() {
-    if (n_ == 1) return;
+    if (n_ == 1 || !pool_) return;
     for (int b = 0; b < n_; ++b)
       if (cudaEventRecord(pool_->join[b], pool_->s[b]) == cudaSuccess) cudaStreamWaitEvent(st_, pool_->join[b], 0);
   }

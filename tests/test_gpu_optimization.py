@@ -104,3 +104,32 @@ def test_optimize_sgd_matches_host_loop(cuda_lib):
         u, _ = R.update(R.Rule("sgd", 0.05), g.cpu().numpy(), R.init(th))
         th = R.apply(th, u)
         assert np.array_equal(P[k + 1].cpu().numpy(), th)
+
+
+def test_overlapped_loops_equal_one_by_one(study_results):
+    """run_all enqueues the four loops from four host threads onto four
+    streams; each loop's objectives and parameters equal its own loop run
+    alone (bitwise: each has its own workspace and the same kernels)."""
+    study, res, _ = study_results
+    for cfg in study.optim_configs:
+        alone = study._run_single_optimizer(cfg["name"], cfg["optimizer"])
+        assert np.array_equal(alone["history"]["objectives"], res[cfg["name"]]["history"]["objectives"])
+        assert np.array_equal(alone["history"]["parameters"], res[cfg["name"]]["history"]["parameters"])
+
+
+def test_overlapped_loops_raise_on_the_callers_thread(study_results):
+    """An error while one loop is enqueued (on its own thread) is raised to
+    the caller of run_all, after the other loops' threads have finished."""
+    from ns_solver_jax_differential_distributed_gb300 import optimization as opt
+    study = study_results[0]
+
+    class Broken:
+        def native(self):
+            raise RuntimeError("broken optimiser spec")
+
+    cfgs = [study.optim_configs[0], {"name": "broken", "optimizer": Broken()}]
+    mixed = opt.ParameterOptimizationStudy(study.objective, study.grad_jax, [1.0, 0.5], optim_configs=cfgs,
+                                           optim_steps=2)
+    with pytest.raises(RuntimeError, match="broken optimiser spec"):
+        mixed.run_all()
+    torch.cuda.synchronize()
