@@ -57,6 +57,10 @@ class Ensemble:
                 autotune.apply_cached(N, L, scheme, self.device)
         self.u0 = [torch.from_numpy(np.ascontiguousarray(s.u0, dtype=np.float32)).to(self.device)
                    for s in self.specs]
+        for k, (s, u) in enumerate(zip(self.specs, self.u0)):
+            # the kernels read each member's field through a bare pointer
+            if tuple(u.shape) != (2, s.N, s.N):
+                raise ValueError(f"member {k}: u0 must have shape (2, {s.N}, {s.N}), got {tuple(u.shape)}")
         self.theta = [torch.from_numpy(np.asarray(s.theta, dtype=np.float32)).to(self.device)
                       for s in self.specs]
         self.u_final = [torch.empty_like(u) for u in self.u0]

@@ -186,6 +186,42 @@ class Server:
     def _initial(self, r: Request) -> torch.Tensor:
         return r.u0 if r.u0 is not None else self.u0.get(r.N, r.seed)
 
+    def _prepare(self, r: Request) -> None:
+        """Checks of a request's own arguments on arrival, so that a bad
+        request fails alone instead of stopping the batch it would join: its
+        kind, scheme, dt, nu and L (the C ABI's rules), steps >= 1, an N the
+        kernels support, theta of 2 or 3 entries (kept as float32; none means
+        the reference's default [1, 0.5]) and an explicit u0 of shape
+        (2, N, N) in float32 on the server's device (copied when it is not
+        contiguous or not 16-byte aligned)."""
+        if r.kind not in ("forward", "grad"):
+            raise ValueError(f"kind must be 'forward' or 'grad', got {r.kind!r}")
+        _native.make_phys(r.L, r.nu, r.dt, r.scheme)  # raises on an unknown scheme
+        for name, v in (("dt", r.dt), ("L", r.L)):
+            if not (math.isfinite(v) and v > 0):
+                raise ValueError(f"{name} must be positive and finite, got {v}")
+        if not math.isfinite(r.nu):
+            raise ValueError(f"nu must be finite, got {r.nu}")
+        if int(r.steps) < 1:
+            raise ValueError(f"steps must be >= 1, got {r.steps}")
+        th = np.asarray([1.0, 0.5] if r.theta is None else r.theta, dtype=np.float32).reshape(-1)
+        if th.size not in (2, 3):
+            raise ValueError(f"theta must have 2 or 3 entries, got {th.size}")
+        r.theta = th
+        _native.get_plan(r.N, r.L, self.device)  # raises on an unsupported N
+        if r.u0 is not None:
+            u0 = _native._cuda_f32(r.u0, "u0")
+            if tuple(u0.shape) != (2, r.N, r.N) or u0.device != self.device:
+                raise ValueError(f"u0 must be a (2, {r.N}, {r.N}) tensor on {self.device}, got "
+                                 f"{tuple(u0.shape)} on {u0.device}")
+            r.u0 = u0
+
+    def _fail(self, r: Request, exc: BaseException, t0: float, completed: list) -> None:
+        r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
+        r.t_done = time.perf_counter() - t0
+        completed.append(r)
+        self.stats["failed"] += 1
+
     # -- memory accounting
     def _fwd_bytes(self, r: Request) -> int:
         plan = _native.get_plan(r.N, r.L, self.device)
@@ -278,8 +314,14 @@ class Server:
         while True:
             now = time.perf_counter() - t0
             while nxt < len(reqs) and (not realtime or reqs[nxt].arrival <= now):
-                pending.append(reqs[nxt])
+                r = reqs[nxt]
                 nxt += 1
+                try:
+                    self._prepare(r)
+                except Exception as exc:  # this request fails; nothing was charged
+                    self._fail(r, exc, t0, completed)
+                    continue
+                pending.append(r)
             # admission (FIFO): memory budget, and a cap on active forward work
             act_cells = sum(a["r"].N ** 2 for a in active)
             grad_cells = sum(a["r"].N ** 2 for a in gactive)
@@ -307,10 +349,7 @@ class Server:
                     try:
                         entry = self._admit_grad(r, gstream)
                     except Exception as exc:  # this request fails; nothing was charged
-                        r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
-                        r.t_done = time.perf_counter() - t0
-                        completed.append(r)
-                        self.stats["failed"] += 1
+                        self._fail(r, exc, t0, completed)
                         continue
                     entry["nb"] = nb
                     self.used += nb
@@ -330,10 +369,7 @@ class Server:
                         Jt = self._alloc(r, (), torch.float32)
                         th = torch.from_numpy(r.theta).to(self.device)
                     except Exception as exc:  # this request fails; nothing was charged
-                        r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
-                        r.t_done = time.perf_counter() - t0
-                        completed.append(r)
-                        self.stats["failed"] += 1
+                        self._fail(r, exc, t0, completed)
                         continue
                     self.used += nb
                     active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=0, nb=nb, plan=plan))
@@ -376,11 +412,17 @@ class Server:
                     arr[k].state = a["state"].data_ptr()
                     arr[k].total_steps = r.steps
                     arr[k].done_steps = a["done"]
-                need = L.nsgb_ensemble_workspace_bytes(arr, len(active))
-                if ws is None or ws.numel() < need:
-                    ws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
-                _native.check("nsgb_ensemble_advance", L.nsgb_ensemble_advance(
-                    arr, len(active), self.slice, ws.data_ptr(), ws.numel(), stream.cuda_stream))
+                try:
+                    need = L.nsgb_ensemble_workspace_bytes(arr, len(active))
+                    if ws is None or ws.numel() < need:
+                        ws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
+                    _native.check("nsgb_ensemble_advance", L.nsgb_ensemble_advance(
+                        arr, len(active), self.slice, ws.data_ptr(), ws.numel(), stream.cuda_stream))
+                except Exception as exc:  # the tick's requests fail; the server serves on
+                    for a in active:
+                        self.used -= a["nb"]
+                        self._fail(a["r"], exc, t0, completed)
+                    active = []
                 keep = []
                 for a in active:
                     a["done"] = min(a["r"].steps, a["done"] + self.slice)
@@ -405,10 +447,18 @@ class Server:
                 arr = (_native.GradMember * len(gactive))(*[a["m"] for a in gactive])
                 need = L.nsgb_grad_batch_workspace_bytes(len(gactive), self.grad_slice)
                 with torch.cuda.stream(gstream):
-                    if gws is None or gws.numel() < need:
-                        gws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
-                    _native.check("nsgb_grad_batch_advance", L.nsgb_grad_batch_advance(
-                        arr, len(gactive), self.grad_slice, gws.data_ptr(), gws.numel(), gstream.cuda_stream))
+                    try:
+                        if gws is None or gws.numel() < need:
+                            gws = torch.empty(max(need, 1 << 20), dtype=torch.uint8, device=self.device)
+                        _native.check("nsgb_grad_batch_advance", L.nsgb_grad_batch_advance(
+                            arr, len(gactive), self.grad_slice, gws.data_ptr(), gws.numel(),
+                            gstream.cuda_stream))
+                    except Exception as exc:  # the tick's requests fail; the server serves on
+                        for a in gactive:
+                            self.used -= a["nb"]
+                            grads_inflight -= 1
+                            self._fail(a["r"], exc, t0, completed)
+                        gactive = []
                     keep = []
                     for a in gactive:
                         a["m"].done_ops = min(a["total"], a["m"].done_ops + self.grad_slice)

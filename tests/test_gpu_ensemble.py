@@ -75,3 +75,13 @@ def test_ensemble_single_step_and_one_member(ens_mod):
         J, us = ens.run()
         Js, uss = ens.run_sequential()
         assert torch.equal(J, Js) and torch.equal(us[0], uss[0])
+
+
+def test_ensemble_rejects_a_field_of_the_wrong_size(ens_mod):
+    """Members reach the kernels as bare pointers, so a u0 whose shape is not
+    (2, N, N) is refused before anything is allocated or launched."""
+    import dataclasses
+    specs = _specs(ens_mod, count=3, sizes=(32, 64), probs=(0.5, 0.5))
+    bad = dataclasses.replace(specs[1], u0=np.zeros((2, specs[1].N // 2, specs[1].N // 2), np.float32))
+    with pytest.raises(ValueError, match="member 1: u0 must have shape"):
+        ens_mod.Ensemble([specs[0], bad, specs[2]], steps=2)

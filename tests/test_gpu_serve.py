@@ -103,6 +103,83 @@ def test_failures_are_isolated(serve):
     assert s["statuses"] == {"ok": len(reqs) - 5, "nonfinite": 2, "failed": 2, "cancelled": 1}
 
 
+def _clean_run(serve, n):
+    srv = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128, grad_workers=2)
+    ref, _ = srv.run(_trace(serve, n), realtime=False)
+    return {r.rid: r for r in ref}
+
+
+def _assert_like(r, ref):
+    assert r.status == "ok" and r.J == ref.J, r.rid
+    if r.kind == "grad":
+        assert np.array_equal(r.grad, ref.grad), r.rid
+    else:
+        assert torch.equal(r.u_final, ref.u_final), r.rid
+
+
+def test_bad_requests_fail_alone(serve):
+    """Requests with arguments the solver refuses (an unsupported N, an
+    unknown scheme, dt = 0, a u0 of the wrong shape, theta of 4 entries) fail
+    on arrival with their reason; a float64 theta is taken as float32; every
+    other request completes with the bits of an undisturbed run."""
+    ref = _clean_run(serve, 30)
+    reqs = _trace(serve, 30)
+    fwd = [r for r in reqs if r.kind == "forward"]
+    grd = [r for r in reqs if r.kind == "grad"]
+    bad = {fwd[0].rid: "N=100 unsupported", grd[0].rid: "scheme", fwd[2].rid: "dt must be",
+           fwd[4].rid: "u0 must be", grd[1].rid: "theta must have"}
+    fwd[0].N = 100
+    grd[0].scheme = "lax-wendroff"
+    fwd[2].dt = 0.0
+    fwd[4].u0 = torch.zeros(2, fwd[4].N // 2, fwd[4].N // 2, device="cuda")
+    grd[1].theta = np.array([1.0, 0.5, 1e-3, 7.0], np.float32)
+    f64 = fwd[6]
+    f64.theta = np.asarray(f64.theta, np.float64)
+    srv = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128, grad_workers=2)
+    done, _ = srv.run(reqs, realtime=False)
+    assert len(done) == len(reqs)
+    assert srv.used == pytest.approx(0.0)
+    for r in done:
+        if r.rid in bad:
+            assert r.status == "failed" and bad[r.rid].lower() in r.error.lower(), (r.rid, r.error)
+        else:
+            _assert_like(r, ref[r.rid])
+
+
+def test_failed_tick_fails_only_its_requests(serve, monkeypatch):
+    """A batched tick whose call reports an error (injected on the first
+    forward tick and the first gradient tick) fails the requests in that tick
+    only; the server serves on, and every later request completes with the
+    bits of an undisturbed run."""
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    ref = _clean_run(serve, 30)
+    real_check = _native.check
+    hit = set()
+
+    def check(name, status):
+        real_check(name, status)
+        if name in ("nsgb_ensemble_advance", "nsgb_grad_batch_advance") and name not in hit:
+            hit.add(name)
+            raise RuntimeError(f"injected failure of {name}")
+
+    monkeypatch.setattr(_native, "check", check)
+    srv = serve.Server(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128,
+                       max_active_grad_cells=2 * 128 * 128)
+    reqs = _trace(serve, 30)
+    done, _ = srv.run(reqs, realtime=False)
+    torch.cuda.synchronize()
+    assert hit == {"nsgb_ensemble_advance", "nsgb_grad_batch_advance"}
+    assert len(done) == len(reqs)
+    assert srv.used == pytest.approx(0.0)
+    failed = [r for r in done if r.status == "failed"]
+    assert failed and all("injected" in r.error for r in failed)
+    assert {r.kind for r in failed} == {"forward", "grad"}
+    assert {r.kind for r in done if r.status == "ok"} == {"forward", "grad"}
+    for r in done:
+        if r.status != "failed":
+            _assert_like(r, ref[r.rid])
+
+
 def test_batched_and_worker_gradients_agree(serve):
     """Gradient requests served by the batched path (several in flight at
     once, work split into uneven slices) and by worker threads running
