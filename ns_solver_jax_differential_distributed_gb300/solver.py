@@ -450,8 +450,15 @@ class SingleCoreNSSolver:
         if torch.is_grad_enabled() and (
                 (isinstance(th, torch.Tensor) and th.requires_grad) or
                 (isinstance(u0t, torch.Tensor) and u0t.requires_grad)):
-            th_d = th.to(self.device, torch.float32)
+            th_d = th.to(self.device, torch.float32).reshape(-1)
             u0_d = u0t.to(self.device, torch.float32)
+            # the same checks as the plain path (the session would otherwise
+            # take N from u0)
+            if th_d.numel() not in (2, 3):
+                raise ValueError(f"theta must have 2 or 3 entries, got {th_d.numel()}")
+            N = self.grid.N
+            if tuple(u0_d.shape) != (2, N, N):
+                raise ValueError(f"u must have shape (2, {N}, {N}), got {tuple(u0_d.shape)}")
             return _RolloutFn.apply(th_d, u0_d, self, self._every())
         th = self._theta(th)
         u0t = self._u(u0t)

@@ -121,6 +121,23 @@ def test_autograd_function(nsgb):
     assert not uf.requires_grad
 
 
+def test_autograd_path_checks_shapes(nsgb):
+    """The differentiable rollout refuses what the plain rollout refuses: a
+    u0 of another grid size and a theta of 4 entries."""
+    N, L = 32, 2 * math.pi
+    s = make_solver(nsgb, N, L, 1e-3, 1e-3, 4, "central")
+    th = torch.tensor([1.0, 0.5], device="cuda", requires_grad=True)
+    small = torch.zeros(2, N // 2, N // 2, device="cuda", requires_grad=True)
+    with pytest.raises(ValueError, match="u must have shape"):
+        s.rollout(small, th)
+    u0 = torch.zeros(2, N, N, device="cuda")
+    with pytest.raises(ValueError, match="theta must have 2 or 3 entries"):
+        s.rollout(u0, torch.ones(4, device="cuda", requires_grad=True))
+    J, _ = s.rollout(u0, th.reshape(1, 2))  # any shape with 2 entries, as the plain path
+    J.backward()
+    assert th.grad.shape == (2,)
+
+
 def test_two_entry_theta(nsgb):
     """The reference's 2-entry theta: gradient has 2 entries, matches the
     3-entry call's first two."""
