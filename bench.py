@@ -722,7 +722,7 @@ def run_serve(args):
     torch.cuda.synchronize(dev)
     clocks = ClockSampler(0).start()
     t0 = time.perf_counter()
-    done, trace = srv.run(reqs, realtime=True, drain_limit=30.0)
+    done, trace = srv.run(reqs, realtime=True, drain_limit=30.0, suspend=False)
     wall = time.perf_counter() - t0
     clock_info = clocks.stop()
     summ = serve.summarize(reqs, done, wall)
@@ -732,7 +732,8 @@ def run_serve(args):
     summ.update({"metric": "served solves/s", "rate_req_per_s": args.rate, "duration_s": args.duration,
                  "max_queue": max(q[1] for q in trace) if trace else 0,
                  "queue_at_end": trace[-1][1] if trace else 0,
-                 "grad_fraction_completed": sum(r.kind == "grad" for r in done) / max(1, len(done)),
+                 "grad_fraction_completed": (sum(r.kind == "grad" for r in done if r.status == "ok")
+                                             / max(1, sum(r.status == "ok" for r in done))),
                  "plain_per_request": plain,
                  "speedup_vs_plain": summ["solves_per_s"] / plain["solves_per_s"],
                  "clocks": clock_info,

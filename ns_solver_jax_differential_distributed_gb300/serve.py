@@ -25,8 +25,16 @@ initial state; NSGB_ERR_NONFINITE of the C ABI), "failed" (its allocation or
 its solve raised; ``error`` says why) or "cancelled" (``Server.cancel``) --
 and the others carry on with the same results as when served alone.
 
+``Server.stop`` ends a run gracefully: the active forward and batched
+gradient requests are suspended to host memory (status "suspended", their
+device state, J and progress in ``Request.resume``), requests not yet
+admitted come back with status "queued", and a later ``run`` given them
+resumes each where it stopped, with the bits of an uninterrupted solve.  A
+run that reaches its drain limit ends the same way.
+
 Latency is measured from arrival to the moment the result (J, and dJ/dtheta
-for gradient requests) is on the host.  Results do not depend on what else
+for gradient requests) is on the host; for a resumed request, from the start
+of the run that resumed it.  Results do not depend on what else
 is in flight: a request's arithmetic is that of a plain solve, which the
 tests check bit for bit.
 """
@@ -67,9 +75,12 @@ class Request:
     u_final: torch.Tensor = field(default=None, repr=False)
     t_admit: float = None
     t_done: float = None
-    status: str = None      # "ok", "nonfinite", "failed", "cancelled"
+    status: str = None      # "ok", "nonfinite", "failed", "cancelled", "suspended", "queued"
     error: str = None
     u0: torch.Tensor = field(default=None, repr=False)  # explicit initial state (else seeded)
+    # a suspended request's host checkpoint: its device state, J, progress
+    # (steps or gradient operations done) and the launch shapes it ran with
+    resume: dict = field(default=None, repr=False)
 
     @property
     def cells(self) -> int:
@@ -165,6 +176,7 @@ class Server:
         self.stats = collections.Counter()
         self._lock = threading.Lock()
         self._cancel = set()
+        self._stop = False
 
     def cancel(self, rid: int) -> None:
         """Cancel request `rid`: dropped if still queued or advancing in a
@@ -177,6 +189,50 @@ class Server:
     def _cancelled(self, r: Request) -> bool:
         with self._lock:
             return r.rid in self._cancel
+
+    def stop(self) -> None:
+        """Ask the running ``run`` (any thread may call this) to stop at its
+        next pass: it admits nothing more, suspends its active forward and
+        batched gradient requests to host memory, lets gradients already on
+        worker threads finish, and returns every request it was given, the
+        unfinished ones with status "suspended" or "queued"."""
+        with self._lock:
+            self._stop = True
+
+    def _stopping(self) -> bool:
+        with self._lock:
+            return self._stop
+
+    # -- checkpoints of suspended requests
+    @staticmethod
+    def _shapes(plan) -> tuple:
+        # the objective partials are laid out by the stencil's launch shape,
+        # so a state resumes only under the shapes it was written with
+        return (plan.tiles(), plan.fft_radix(), plan.adjoint_tiles(), plan.fused_rows())
+
+    def _suspend(self, r: Request, plan, state: torch.Tensor, J: torch.Tensor, progress: int, stream) -> None:
+        host = torch.empty(state.shape, dtype=torch.uint8, pin_memory=True)
+        Jh = torch.empty((), dtype=torch.float32, pin_memory=True)
+        with torch.cuda.stream(stream):
+            host.copy_(state, non_blocking=True)
+            Jh.copy_(J, non_blocking=True)
+        r.resume = {"state": host, "J": Jh, "progress": int(progress), "shapes": self._shapes(plan)}
+        r.status, r.t_done = "suspended", None
+
+    def _restore(self, r: Request, plan, state: torch.Tensor, J: torch.Tensor, stream) -> int:
+        """Copy a suspended request's checkpoint into its new device state;
+        returns its progress."""
+        res = r.resume
+        if res["shapes"] != self._shapes(plan):
+            raise RuntimeError(f"the launch shapes of N={r.N} changed since request {r.rid} was suspended "
+                               f"({res['shapes']} -> {self._shapes(plan)})")
+        if res["state"].numel() != state.numel():
+            raise RuntimeError(f"request {r.rid}: checkpoint of {res['state'].numel()} bytes, "
+                               f"state of {state.numel()}")
+        with torch.cuda.stream(stream):
+            state.copy_(res["state"], non_blocking=True)
+            J.copy_(res["J"], non_blocking=True)
+        return int(res["progress"])
 
     def _alloc(self, r: Request, shape, dtype) -> torch.Tensor:
         """Device allocation of a request's resident fields (a test may
@@ -277,14 +333,21 @@ class Server:
         m.steps, m.every = r.steps, GRAD_EVERY
         m.J, m.u_final, m.dJdtheta, m.dJdu0 = J.data_ptr(), None, g.data_ptr(), None
         m.state = state.data_ptr()
-        m.done_ops = 0
+        m.done_ops = self._restore(r, plan, state, J, gstream) if r.resume is not None else 0
         return dict(r=r, m=m, state=state, th=th, J=J, g=g, u0=u0, plan=plan,
                     total=int(L.nsgb_grad_ops(r.steps, GRAD_EVERY)))
 
-    def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None):
+    def run(self, requests, realtime: bool = True, drain_limit: float = None, t0: float = None,
+            suspend: bool = True):
         """Serve `requests` (sorted by arrival).  With realtime, arrivals
         follow the wall clock; otherwise all are available at once.  Stops
-        when all are done or `drain_limit` seconds after the last arrival."""
+        when all are done, `drain_limit` seconds after the last arrival, or
+        after ``stop()``; returns (requests, queue trace) with every request
+        given, those left unfinished as "suspended" (a host checkpoint in
+        ``resume``) or "queued".  Suspended requests passed again resume
+        where they stopped (a gradient request served by worker threads
+        starts over).  With ``suspend=False`` the active requests come back
+        "queued", without host copies, and start over when passed again."""
         reqs = sorted(requests, key=lambda r: r.arrival)
         pending = collections.deque()
         nxt = 0
@@ -311,7 +374,58 @@ class Server:
         completed = []
         queue_trace = []
         ticks = collections.deque()  # events of the ticks still on the GPU
+
+        def collect():
+            """Requests whose work has finished on the device."""
+            nonlocal finishing, gfinishing, grads_inflight
+            still = []
+            for ev, a in finishing:
+                if ev.query():
+                    r = a["r"]
+                    r.J = float(a["J_host"])
+                    r.u_final = a["out"]
+                    r.status = "ok" if math.isfinite(r.J) else "nonfinite"
+                    r.t_done, r.resume = time.perf_counter() - t0, None
+                    self.used -= a["nb"]
+                    completed.append(r)
+                else:
+                    still.append((ev, a))
+            finishing = still
+            still = []
+            for ev, a, Jh, gh in gfinishing:
+                if ev.query():
+                    r = a["r"]
+                    r.J, r.grad = float(Jh), gh.numpy().copy()
+                    if self._cancelled(r):
+                        r.status = "cancelled"
+                    else:
+                        ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
+                        r.status = "ok" if ok else "nonfinite"
+                    r.t_done, r.resume = time.perf_counter() - t0, None
+                    self.used -= a["nb"]
+                    grads_inflight -= 1
+                    completed.append(r)
+                else:
+                    still.append((ev, a, Jh, gh))
+            gfinishing = still
+            while not grad_done.empty():
+                r, nb, exc = grad_done.get()
+                if exc is not None:
+                    r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
+                    self.stats["failed"] += 1
+                elif self._cancelled(r):
+                    r.status = "cancelled"
+                else:
+                    ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
+                    r.status = "ok" if ok else "nonfinite"
+                r.t_done, r.resume = time.perf_counter() - t0, None
+                self.used -= nb
+                grads_inflight -= 1
+                completed.append(r)
+
         while True:
+            if self._stopping():
+                break
             now = time.perf_counter() - t0
             while nxt < len(reqs) and (not realtime or reqs[nxt].arrival <= now):
                 r = reqs[nxt]
@@ -368,11 +482,12 @@ class Server:
                         out = self._alloc(r, (2, r.N, r.N), torch.float32)
                         Jt = self._alloc(r, (), torch.float32)
                         th = torch.from_numpy(r.theta).to(self.device)
+                        done0 = self._restore(r, plan, state, Jt, stream) if r.resume is not None else 0
                     except Exception as exc:  # this request fails; nothing was charged
                         self._fail(r, exc, t0, completed)
                         continue
                     self.used += nb
-                    active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=0, nb=nb, plan=plan))
+                    active.append(dict(r=r, state=state, out=out, J=Jt, th=th, done=done0, nb=nb, plan=plan))
                     act_cells += r.N ** 2
                 self.peak_used = max(self.peak_used, self.used)
             # cancelled requests leave before the next tick
@@ -477,51 +592,7 @@ class Server:
                     gticks.append(tev)
                 if len(gticks) > 2:
                     gticks.popleft().synchronize()
-            # completions
-            still = []
-            for ev, a in finishing:
-                if ev.query():
-                    r = a["r"]
-                    r.J = float(a["J_host"])
-                    r.u_final = a["out"]
-                    r.status = "ok" if math.isfinite(r.J) else "nonfinite"
-                    r.t_done = time.perf_counter() - t0
-                    self.used -= a["nb"]
-                    completed.append(r)
-                else:
-                    still.append((ev, a))
-            finishing = still
-            still = []
-            for ev, a, Jh, gh in gfinishing:
-                if ev.query():
-                    r = a["r"]
-                    r.J, r.grad = float(Jh), gh.numpy().copy()
-                    if self._cancelled(r):
-                        r.status = "cancelled"
-                    else:
-                        ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
-                        r.status = "ok" if ok else "nonfinite"
-                    r.t_done = time.perf_counter() - t0
-                    self.used -= a["nb"]
-                    grads_inflight -= 1
-                    completed.append(r)
-                else:
-                    still.append((ev, a, Jh, gh))
-            gfinishing = still
-            while not grad_done.empty():
-                r, nb, exc = grad_done.get()
-                if exc is not None:
-                    r.status, r.error = "failed", f"{type(exc).__name__}: {exc}"
-                    self.stats["failed"] += 1
-                elif self._cancelled(r):
-                    r.status = "cancelled"
-                else:
-                    ok = math.isfinite(r.J) and bool(np.all(np.isfinite(r.grad)))
-                    r.status = "ok" if ok else "nonfinite"
-                r.t_done = time.perf_counter() - t0
-                self.used -= nb
-                grads_inflight -= 1
-                completed.append(r)
+            collect()
             queue_trace.append((now, len(pending), len(active), grads_inflight))
             all_in = nxt >= len(reqs)
             if all_in and not pending and not active and not finishing and grads_inflight == 0:
@@ -530,9 +601,49 @@ class Server:
                 break
             if not active and not finishing and not gactive and not gfinishing:
                 time.sleep(0.0005)
+        # The run ends: the active requests are suspended to host memory (their
+        # copies follow their last tick on its stream), gradients waiting for a
+        # worker thread go back to the queue, the running ones finish, and what
+        # has finished on the device is collected.
+        for a in active:
+            if suspend:
+                self._suspend(a["r"], a["plan"], a["state"], a["J"], a["done"], stream)
+                completed.append(a["r"])
+            else:
+                pending.append(a["r"])
+            self.used -= a["nb"]
+        for a in gactive:
+            if suspend:
+                self._suspend(a["r"], a["plan"], a["state"], a["J"], a["m"].done_ops, gstream)
+                completed.append(a["r"])
+            else:
+                pending.append(a["r"])
+            self.used -= a["nb"]
+            grads_inflight -= 1
+        active, gactive = [], []
+        while True:
+            try:
+                item = grad_q.get_nowait()
+            except queue.Empty:
+                break
+            r, nb = item
+            self.used -= nb
+            grads_inflight -= 1
+            pending.append(r)
         for _ in workers:
             grad_q.put(None)
+        for w in workers:
+            w.join()
         torch.cuda.synchronize(self.device)
+        collect()
+        for r in list(pending) + reqs[nxt:]:
+            if self._cancelled(r):
+                r.status, r.t_done = "cancelled", time.perf_counter() - t0
+            else:
+                r.status, r.t_done = ("suspended" if r.resume is not None else "queued"), None
+            completed.append(r)
+        with self._lock:
+            self._stop = False
         return completed, queue_trace
 
 

@@ -180,6 +180,60 @@ def test_failed_tick_fails_only_its_requests(serve, monkeypatch):
             _assert_like(r, ref[r.rid])
 
 
+@pytest.mark.parametrize("grad_mode", ["batched", "workers"])
+def test_stop_suspends_and_resume_gives_the_same_bits(serve, monkeypatch, grad_mode):
+    """Server.stop() in the middle of a run suspends the active requests to
+    host memory and returns the rest as queued; a new server given them
+    finishes every request with the bits of an uninterrupted run.  A
+    checkpoint whose launch shapes no longer match is refused."""
+    from ns_solver_jax_differential_distributed_gb300 import _native
+    ref = _clean_run(serve, 30)
+    kw = dict(hbm_budget=2e9, slice_steps=7, max_active_cells=3 * 128 * 128,
+              max_active_grad_cells=2 * 128 * 128, grad_slice_ops=16, grad_mode=grad_mode, grad_workers=2)
+    srv = serve.Server(**kw)
+    real_check = _native.check
+    trigger = "nsgb_grad_batch_advance" if grad_mode == "batched" else "nsgb_ensemble_advance"
+    calls = [0]
+
+    def check(name, status):
+        real_check(name, status)
+        if name == trigger:
+            calls[0] += 1
+            if calls[0] == 3:
+                srv.stop()
+
+    monkeypatch.setattr(_native, "check", check)
+    reqs = _trace(serve, 30)
+    done, _ = srv.run(reqs, realtime=False)
+    monkeypatch.setattr(_native, "check", real_check)
+    assert calls[0] == 3 and len(done) == len(reqs)
+    assert srv.used == pytest.approx(0.0)
+    sus = [r for r in done if r.status == "suspended"]
+    rest = [r for r in done if r.status in ("suspended", "queued")]
+    kinds = {"forward", "grad"} if grad_mode == "batched" else {"forward"}
+    assert {r.kind for r in sus} == kinds
+    assert all(0 < r.resume["progress"] for r in sus)
+    assert any(r.status == "queued" for r in rest)
+    # a checkpoint written under other launch shapes is refused
+    odd = sus[0]
+    saved = odd.resume
+    odd.resume = dict(saved, shapes=((0, 0, 0, 0),) + tuple(saved["shapes"][1:]))
+    srv2 = serve.Server(**kw)
+    done2, _ = srv2.run(rest, realtime=False)
+    assert srv2.used == pytest.approx(0.0)
+    by = {r.rid: r for r in done2}
+    assert by[odd.rid].status == "failed" and "launch shapes" in by[odd.rid].error
+    odd.resume = saved
+    (again,), _ = serve.Server(**kw).run([odd], realtime=False)
+    final = {r.rid: r for r in done if r.status not in ("suspended", "queued")}
+    final.update(by)
+    final[odd.rid] = again
+    assert len(final) == len(reqs)
+    for rid, r in final.items():
+        _assert_like(r, ref[rid])
+        assert r.resume is None
+
+
 def test_batched_and_worker_gradients_agree(serve):
     """Gradient requests served by the batched path (several in flight at
     once, work split into uneven slices) and by worker threads running
