@@ -605,19 +605,24 @@ class Server:
         # copies follow their last tick on its stream), gradients waiting for a
         # worker thread go back to the queue, the running ones finish, and what
         # has finished on the device is collected.
-        for a in active:
+        def park(a, progress, st):
+            # a request whose checkpoint cannot be taken (no pinned host
+            # memory) keeps its previous checkpoint if it has one, else comes
+            # back queued and starts over
             if suspend:
-                self._suspend(a["r"], a["plan"], a["state"], a["J"], a["done"], stream)
-                completed.append(a["r"])
-            else:
-                pending.append(a["r"])
+                try:
+                    self._suspend(a["r"], a["plan"], a["state"], a["J"], progress, st)
+                    completed.append(a["r"])
+                    return
+                except Exception as exc:
+                    a["r"].error = f"checkpoint failed: {type(exc).__name__}: {exc}"
+            pending.append(a["r"])
+
+        for a in active:
+            park(a, a["done"], stream)
             self.used -= a["nb"]
         for a in gactive:
-            if suspend:
-                self._suspend(a["r"], a["plan"], a["state"], a["J"], a["m"].done_ops, gstream)
-                completed.append(a["r"])
-            else:
-                pending.append(a["r"])
+            park(a, a["m"].done_ops, gstream)
             self.used -= a["nb"]
             grads_inflight -= 1
         active, gactive = [], []
