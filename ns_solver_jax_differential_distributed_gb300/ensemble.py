@@ -221,14 +221,19 @@ class GradientBatch:
         u0 = _native._cuda_f32(torch.as_tensor(u0, dtype=torch.float32).to(self.device), "u0")
         theta = _native._cuda_f32(torch.as_tensor(theta, dtype=torch.float32).to(self.device), "theta")
         N = _native._square(u0, "u0", 2)
-        plan = _native.get_plan(N, L, self.device)
+        if theta.numel() not in (2, 3):
+            raise ValueError(f"theta must have 2 or 3 entries, got {theta.numel()}")
         steps, every = int(steps), int(every)
+        if steps < 1 or every < 1:
+            raise ValueError(f"steps and every must be >= 1, got {steps} and {every}")
+        phys = _native.make_phys(L, nu, dt, scheme, mu0, sigma0, C)
+        plan = _native.get_plan(N, L, self.device)
         lib = _bind()
         state = torch.empty(lib.nsgb_rollout_grad_workspace_bytes(plan.handle, steps, every),
                             dtype=torch.uint8, device=self.device)
         m = _native.GradMember()
         m.plan = plan.handle.value
-        m.phys = _native.make_phys(L, nu, dt, scheme, mu0, sigma0, C)
+        m.phys = phys
         rec = {
             "u0": u0, "theta": theta, "plan": plan, "state": state,
             "J": torch.empty((), dtype=torch.float32, device=self.device),
@@ -278,16 +283,23 @@ class GradientBatch:
         while self.pending():
             self.advance(ops_per_call)
 
-    def result(self, sid: int):
+    def _finished(self, sid: int) -> dict:
         r = self._solves[sid]
+        if r["member"].done_ops < r["total"]:
+            raise RuntimeError(f"gradient solve {sid} has done {r['member'].done_ops} of its "
+                               f"{r['total']} operations")
+        return r
+
+    def result(self, sid: int):
+        r = self._finished(sid)
         return r["J"], r["g"]
 
     def du0(self, sid: int):
-        return self._solves[sid]["du0"]
+        return self._finished(sid)["du0"]
 
     def u_final(self, sid: int):
         """The final state (written when the forward phase ends)."""
-        return self._solves[sid]["u_final"]
+        return self._finished(sid)["u_final"]
 
     def release(self, sid: int):
         """Frees a finished (or abandoned) solve's device state."""

@@ -151,3 +151,29 @@ def test_u_final_and_two_parameter_theta(mods):
         Jb, gb_ = gb.result(sid)
         assert gb_.numel() == 2
         assert torch.equal(Jb, J) and torch.equal(gb_, g) and torch.equal(gb.u_final(sid), uf)
+
+
+def test_refuses_bad_solves_and_unfinished_reads(mods):
+    """add() refuses a theta of 4 entries, steps or every below 1 and an
+    unknown scheme before allocating anything; results of a solve that has
+    not finished are refused, and are there once it has."""
+    _native, ensemble = mods
+    gb = ensemble.GradientBatch()
+    u0, th = _case(32, 0)
+    with pytest.raises(ValueError, match="theta must have 2 or 3"):
+        gb.add(u0, torch.ones(4, device="cuda"), 4, 2, L, 1e-3, 0.01, "central")
+    for steps, every in ((0, 1), (4, 0)):
+        with pytest.raises(ValueError, match="must be >= 1"):
+            gb.add(u0, th, steps, every, L, 1e-3, 0.01, "central")
+    with pytest.raises(ValueError, match="Unknown advection scheme"):
+        gb.add(u0, th, 4, 2, L, 1e-3, 0.01, "lax")
+    assert gb.pending() == []
+    sid = gb.add(u0, th, 4, 2, L, 1e-3, 0.4 / 32, "central", want_du0=True, want_u_final=True)
+    gb.advance(3)
+    for read in (gb.result, gb.du0, gb.u_final):
+        with pytest.raises(RuntimeError, match="has done 3 of its"):
+            read(sid)
+    gb.run(5)
+    J, g = gb.result(sid)
+    Jr, gr, _ = _reference(_native, u0, th, 32, "central", 4, 2)
+    assert torch.equal(J, Jr) and torch.equal(g, gr)
