@@ -107,7 +107,11 @@ class Ensemble:
         the whole ensemble: the single-solve tuner favours short row bands
         (one solve must fill the GPU), while a batch gets its parallelism from
         its members and prefers taller bands, whose halo overhead is smaller.
-        Largest groups first; FFT shapes stay as tuned for single solves."""
+        Largest groups first; FFT shapes stay as tuned for single solves.
+        The shapes are set on the plans the process shares per grid size, so
+        later solves of those sizes use them too (fields keep their bits; J
+        can change by rounding, its partials following the stencil's blocks);
+        ``autotune.apply_cached`` restores the single-solve shapes."""
         cells = {}
         for s in self.specs:
             cells[(s.N, s.L)] = cells.get((s.N, s.L), 0) + s.N * s.N
