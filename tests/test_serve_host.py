@@ -69,3 +69,17 @@ def test_summarize_counts_only_ok_results():
     n_ok = sum(r.status == "ok" for r in reqs)
     assert s["completed"] == n_ok and s["solves_per_s"] == pytest.approx(n_ok)
     assert sum(s["statuses"].values()) == len(reqs) and s["statuses"]["ok"] == n_ok
+
+
+def test_summarize_reports_unfinished_requests_apart():
+    """Requests a run hands back unfinished ("suspended" with a checkpoint,
+    "queued" without) appear in the status counts, never as completed."""
+    reqs = serve.make_trace(rate=100.0, duration=0.5, seed=6, sizes=(64,), steps_range=(10, 10), p_grad=0.0)
+    for i, r in enumerate(reqs):
+        r.status = ["ok", "suspended", "queued"][i % 3]
+        r.t_done = r.arrival + 0.2 if r.status == "ok" else None
+    s = serve.summarize(reqs, reqs, wall=1.0)
+    n_ok = sum(r.status == "ok" for r in reqs)
+    assert s["completed"] == n_ok
+    assert s["statuses"] == {k: sum(r.status == k for r in reqs) for k in ("ok", "suspended", "queued")}
+    assert s["p50_latency_s"] == pytest.approx(0.2)
