@@ -107,7 +107,9 @@ class Ensemble:
         the whole ensemble: the single-solve tuner favours short row bands
         (one solve must fill the GPU), while a batch gets its parallelism from
         its members and prefers taller bands, whose halo overhead is smaller.
-        Largest groups first; FFT shapes stay as tuned for single solves.
+        Then, per size, the FFT passes' CTA shapes (rows per CTA) the same
+        way; the radix stays as tuned for single solves, so fields keep the
+        bits of single solves.  Largest groups first.
         The shapes are set on the plans the process shares per grid size, so
         later solves of those sizes use them too (fields keep their bits; J
         can change by rounding, its partials following the stencil's blocks);
@@ -133,7 +135,26 @@ class Ensemble:
                 ms = min(self._time_run() for _ in range(2))  # the better of two: less timing noise
                 if best_ms is None or ms < best_ms:
                     best, best_ms = (tw, th), ms
-            plan.set_tiles(best[0], best[1], base[2], base[3])
+            # the FFT passes' CTA shapes for the batch: rows of a row-FFT CTA,
+            # then spectrum rows of a column CTA.  The radix stays and rows
+            # are paired the same way in any shape, so every transform keeps
+            # its bits.
+            shape = [base[2], base[3]]
+            for axis, choices in ((0, autotune.ROW_CHOICES), (1, autotune.COL_CHOICES)):
+                keep, keep_ms = shape[axis], None
+                for v in choices:
+                    trial = list(shape)
+                    trial[axis] = v
+                    try:
+                        plan.set_tiles(best[0], best[1], trial[0], trial[1])
+                    except _native.NativeError:
+                        continue
+                    self._ensure_workspace()
+                    ms = min(self._time_run() for _ in range(2))
+                    if keep_ms is None or ms < keep_ms:
+                        keep, keep_ms = v, ms
+                shape[axis] = keep
+            plan.set_tiles(best[0], best[1], shape[0], shape[1])
             self._ensure_workspace()
 
     @property
