@@ -432,8 +432,28 @@ struct EnsGraph {
 };
 std::mutex g_ens_mu;
 std::vector<EnsGraph> g_ens_graphs;
-cudaStream_t g_ens_streams[9] = {nullptr};
-cudaEvent_t g_ens_events[10] = {nullptr};
+// Streams and events an ensemble chunk graph is captured with, per device
+// (the capture stream and up to 8 branch streams; the fork event and one join
+// event per branch).  Replays run on the caller's stream.
+struct EnsPool {
+  cudaStream_t s[9] = {};
+  cudaEvent_t e[9] = {};
+};
+std::map<int, EnsPool> g_ens_pools;
+
+// The pool of the current device, creating what is missing (a failed creation
+// leaves the rest for the next call to retry).
+int ens_pool(EnsPool*& out) {
+  int dev = 0;
+  NSGB_CUDA(cudaGetDevice(&dev));
+  EnsPool& p = g_ens_pools[dev];
+  for (auto& x : p.s)
+    if (!x) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+  for (auto& x : p.e)
+    if (!x) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+  out = &p;
+  return NSGB_OK;
+}
 
 // Eager fork/join of independent groups of batched launches: the groups'
 // kernels go to branch streams that start after the caller's stream's work so
@@ -1991,28 +2011,26 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
     EnsGraph* eg = nullptr;
     for (auto& g : g_ens_graphs)
       if (g.ws == workspace && g.count == count && g.chunk == chunk && g.sig == sig) eg = &g;
-    if (!g_ens_streams[0]) {
-      for (auto& x : g_ens_streams) NSGB_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
-      for (auto& x : g_ens_events) NSGB_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
-    }
-    cudaStream_t cs = g_ens_streams[0];
     const int nbr = (int)std::min<size_t>(groups.size(), 8);
     if (!eg) {
+      EnsPool* pool = nullptr;
+      if (int r = ens_pool(pool)) return r;
+      cudaStream_t cs = pool->s[0];
       if (g_ens_graphs.size() >= 8) {
         cudaGraphExecDestroy(g_ens_graphs.front().exec);
         g_ens_graphs.erase(g_ens_graphs.begin());
       }
-      std::vector<cudaStream_t> br(g_ens_streams + 1, g_ens_streams + 1 + nbr);
+      std::vector<cudaStream_t> br(pool->s + 1, pool->s + 1 + nbr);
       std::vector<EnsGroup> cg = groups;
       for (auto& G : cg) G.todo = chunk;
       cudaGraph_t graph;
       NSGB_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      cudaError_t ce = cudaEventRecord(g_ens_events[0], cs);
-      for (int b = 0; b < nbr && ce == cudaSuccess; ++b) ce = cudaStreamWaitEvent(br[b], g_ens_events[0], 0);
+      cudaError_t ce = cudaEventRecord(pool->e[0], cs);
+      for (int b = 0; b < nbr && ce == cudaSuccess; ++b) ce = cudaStreamWaitEvent(br[b], pool->e[0], 0);
       for (int k = 0; k < chunk && ce == cudaSuccess; ++k) ce = ensemble_step(cg, dev, k, br);
       for (int b = 0; b < nbr && ce == cudaSuccess; ++b) {
-        ce = cudaEventRecord(g_ens_events[1 + b], br[b]);
-        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, g_ens_events[1 + b], 0);
+        ce = cudaEventRecord(pool->e[1 + b], br[b]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(cs, pool->e[1 + b], 0);
       }
       if (ce == cudaSuccess) ce = launch_counter_batch(dev, count, chunk, true, cs);
       cudaError_t ee = cudaStreamEndCapture(cs, &graph);
@@ -2025,14 +2043,12 @@ int nsgb_ensemble_rollout(const nsgb_member* members_in, int count, int chunk, v
       g_ens_graphs.push_back(g);
       eg = &g_ens_graphs.back();
     }
-    NSGB_CUDA(cudaEventRecord(g_ens_events[9], st));
-    NSGB_CUDA(cudaStreamWaitEvent(cs, g_ens_events[9], 0));
+    // captured on the pool's streams, replayed on the caller's, so ensembles
+    // on different streams overlap on the device
     while (steps - s >= chunk) {
-      NSGB_CUDA(cudaGraphLaunch(eg->exec, cs));
+      NSGB_CUDA(cudaGraphLaunch(eg->exec, st));
       s += chunk;
     }
-    NSGB_CUDA(cudaEventRecord(g_ens_events[9], cs));
-    NSGB_CUDA(cudaStreamWaitEvent(st, g_ens_events[9], 0));
   }
   // remaining steps: the chunks kept the parity (chunk is even)
   for (auto& G : groups) {
@@ -2187,7 +2203,10 @@ int nsgb_time_stages(const nsgb_plan* plan, const nsgb_phys* phys, const float* 
   if (fused) NSGB_CUDA(poisson_fft(plan->N, fused_fft_launch(plan, w.rhs, w.spec, nullptr), st));
   cudaEvent_t e0, e1;
   NSGB_CUDA(cudaEventCreate(&e0));
-  NSGB_CUDA(cudaEventCreate(&e1));
+  if (cudaError_t ce = cudaEventCreate(&e1)) {
+    cudaEventDestroy(e0);
+    return cuda_fail(ce, "cudaEventCreate");
+  }
   double tot[4] = {0, 0, 0, 0};
   cudaError_t err = cudaSuccess;
   for (int stage = 0; stage < 4 && err == cudaSuccess; ++stage) {
