@@ -91,3 +91,23 @@ def test_grad_batch_schedule_and_arguments(lib):
     assert L.nsgb_grad_batch_workspace_bytes(3, 8) > 0
     assert L.nsgb_grad_batch_advance(None, 1, 4, None, 0, None) == 1
     assert b"empty" in L.nsgb_last_error()
+
+
+def test_ensemble_entry_points_refuse_bad_members(lib):
+    """The ensemble calls check their member tables before any device work:
+    an empty table, a NULL plan and steps out of range come back as
+    NSGB_ERR_INVALID_ARG with a message (no GPU is touched)."""
+    L = _native.lib()
+    assert L.nsgb_ensemble_workspace_bytes(None, 0) == 0
+    assert L.nsgb_ensemble_persistent_workspace_bytes(None, 0) == 0
+    for call in (lambda: L.nsgb_ensemble_advance(None, 0, 4, None, 0, None),
+                 lambda: L.nsgb_ensemble_rollout(None, 0, 8, None, 0, None),
+                 lambda: L.nsgb_ensemble_persistent(None, 0, None, 0, None)):
+        assert call() == 1 and b"empty" in L.nsgb_last_error()
+    m = (_native.Member * 1)()
+    m[0].plan = None
+    m[0].phys = _native.make_phys(1.0, 0.01, 1e-3, "central")
+    assert L.nsgb_ensemble_advance(m, 1, 4, None, 0, None) == 1
+    assert b"plan is NULL" in L.nsgb_last_error()
+    gm = (_native.GradMember * 1)()
+    assert L.nsgb_grad_batch_advance(gm, 1, 4, None, 0, None) == 1
